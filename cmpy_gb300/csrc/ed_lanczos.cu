@@ -1,0 +1,587 @@
+// Device Lanczos: the ground state that cmpy obtains from ARPACK eigsh(k=1, which="SA")
+// (cmpy/exactdiag.py:24-43) and the Lanczos coefficients of cmpy/exactdiag.py:324-375,
+// run entirely on the GPU. All scalars (alpha, beta, norms, flags) stay in device memory;
+// the host only enqueues kernels, so control crosses host->device once per solve.
+//
+// Reductions are deterministic: each block writes a partial, the last block to arrive
+// (atomic ticket, no waiting) sums the partials in block order.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ed_plan.cuh"
+
+namespace ed {
+
+constexpr int LZ_NT = 256;
+
+struct LzState {
+  int stop;          // 0 running, 1 converged, 2 invariant subspace
+  int steps;         // size m of the tridiagonal matrix once stopped
+  int status;
+  int pad;
+  double e_prev;     // last convergence-check energy
+  double energy;
+  double residual;
+  double nrm2;       // scratch: last norm^2
+  unsigned int ticket[8];
+};
+
+__device__ __forceinline__ bool lz_stopped(const LzState* st) { return *(volatile const int*)&st->stop != 0; }
+
+// Last-block detection; every thread of the block gets the answer.
+__device__ __forceinline__ bool last_block(unsigned int* ticket) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (am_last) __threadfence();
+  return am_last;
+}
+
+// sum partials[0..n) with the whole block, in a fixed order
+__device__ double block_sum_array(const double* p, int n, double* smem) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += LZ_NT) v += ((volatile const double*)p)[i];
+  return block_sum<LZ_NT>(v, smem);
+}
+
+// ---- start vector ------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+// uniform(0,1) like the reference's np.random.uniform(0, 1) start (exactdiag.py:326), seeded
+__global__ void k_random_start(double* v, int64_t n, uint64_t seed) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = (double)(splitmix64(seed * 0x100000001B3ull + (uint64_t)i) >> 11) * 0x1.0p-53 + 0x1.0p-54;
+}
+
+// out = <a, b> (or ||a||^2 with b == a); result -> *res (and optionally its sqrt -> *res_sqrt)
+__global__ void k_dot(const double* __restrict__ a, const double* __restrict__ b, int64_t n, double* partial,
+                      LzState* st, int tk, double* res, double* res_sqrt, const int* stop) {
+  if (stop && *(volatile const int*)stop) return;
+  __shared__ double sm[LZ_NT / 32];
+  double v = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)LZ_NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * LZ_NT)
+    v = fma(a[i], b[i], v);
+  v = block_sum<LZ_NT>(v, sm);
+  if (threadIdx.x == 0) partial[blockIdx.x] = v;
+  if (last_block(&st->ticket[tk])) {
+    const double s = block_sum_array(partial, gridDim.x, sm);
+    if (threadIdx.x == 0) {
+      *res = s;
+      if (res_sqrt) *res_sqrt = sqrt(s);
+      st->ticket[tk] = 0;
+    }
+  }
+}
+
+// v *= 1/ *scale (scale read from device memory); out may equal v
+__global__ void k_scale(const double* __restrict__ v, double* __restrict__ out, int64_t n, const double* scale,
+                        const int* stop) {
+  if (stop && *(volatile const int*)stop) return;
+  const double s = 1.0 / *scale;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = v[i] * s;
+}
+
+// w -= alpha*q + beta*qprev; norm^2 -> st->nrm2; when final (no reorth) also beta_{k+1}
+// and the breakdown test.
+__global__ void k_lz_update(double* __restrict__ w, const double* __restrict__ q, const double* __restrict__ qp,
+                            int64_t n, const double* alpha_k, const double* beta_k, double* partial, LzState* st,
+                            double* beta_next, int k, int final_norm) {
+  if (lz_stopped(st)) return;
+  __shared__ double sm[LZ_NT / 32];
+  const double a = *alpha_k, b = *beta_k;
+  double v = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)LZ_NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * LZ_NT) {
+    double x = w[i] - a * q[i];
+    if (qp) x -= b * qp[i];
+    w[i] = x;
+    v = fma(x, x, v);
+  }
+  v = block_sum<LZ_NT>(v, sm);
+  if (threadIdx.x == 0) partial[blockIdx.x] = v;
+  if (last_block(&st->ticket[1])) {
+    const double s = block_sum_array(partial, gridDim.x, sm);
+    if (threadIdx.x == 0) {
+      st->nrm2 = s;
+      if (final_norm) {
+        const double bn = sqrt(s);
+        *beta_next = bn;
+        const double scale = fmax(fabs(a), fmax(b, 1e-300));
+        if (!(bn > 1e-13 * scale)) { st->steps = k + 1; st->stop = 2; }
+      }
+      st->ticket[1] = 0;
+    }
+  }
+}
+
+// ---- full reorthogonalisation: classical Gram-Schmidt against Q[0..m) -----------------------
+// partial[j*gridDim + b] = sum_{i in block b} Q[j][i] w[i]; the last block reduces into h[j].
+constexpr int RO_J = 8;  // basis vectors per pass over the w chunk
+__global__ void k_multidot(const double* __restrict__ Q, int64_t ldq, int m, const double* __restrict__ w, int64_t n,
+                           double* partial, double* h, LzState* st) {
+  if (lz_stopped(st)) return;
+  __shared__ double sm[LZ_NT / 32];
+  for (int j0 = 0; j0 < m; j0 += RO_J) {
+    double acc[RO_J];
+#pragma unroll
+    for (int r = 0; r < RO_J; ++r) acc[r] = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)LZ_NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * LZ_NT) {
+      const double wi = w[i];
+#pragma unroll
+      for (int r = 0; r < RO_J; ++r)
+        if (j0 + r < m) acc[r] = fma(Q[(int64_t)(j0 + r) * ldq + i], wi, acc[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < RO_J; ++r) {
+      const double s = block_sum<LZ_NT>(acc[r], sm);
+      if (threadIdx.x == 0 && j0 + r < m) partial[(int64_t)(j0 + r) * gridDim.x + blockIdx.x] = s;
+    }
+  }
+  if (last_block(&st->ticket[2])) {
+    for (int j = 0; j < m; ++j) {
+      const double s = block_sum_array(partial + (int64_t)j * gridDim.x, gridDim.x, sm);
+      if (threadIdx.x == 0) h[j] = s;
+    }
+    if (threadIdx.x == 0) st->ticket[2] = 0;
+  }
+}
+
+// w -= sum_j h[j] Q[j]; optionally accumulates ||w||^2 and finalises beta_{k+1}
+__global__ void k_multiaxpy(const double* __restrict__ Q, int64_t ldq, int m, const double* __restrict__ h,
+                            double* __restrict__ w, int64_t n, double* partial, LzState* st, double* beta_next,
+                            int k, int final_norm, const double* alpha_k) {
+  if (lz_stopped(st)) return;
+  __shared__ double sm[LZ_NT / 32];
+  __shared__ double hs[1024];
+  for (int j = threadIdx.x; j < m && j < 1024; j += LZ_NT) hs[j] = h[j];
+  __syncthreads();
+  double v = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)LZ_NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * LZ_NT) {
+    double x = w[i];
+    for (int j = 0; j < m; ++j) x = fma(-hs[j], Q[(int64_t)j * ldq + i], x);
+    w[i] = x;
+    v = fma(x, x, v);
+  }
+  v = block_sum<LZ_NT>(v, sm);
+  if (threadIdx.x == 0) partial[blockIdx.x] = v;
+  if (last_block(&st->ticket[3])) {
+    const double s = block_sum_array(partial, gridDim.x, sm);
+    if (threadIdx.x == 0) {
+      st->nrm2 = s;
+      if (final_norm) {
+        const double bn = sqrt(s);
+        *beta_next = bn;
+        const double scale = fmax(fabs(*alpha_k), 1e-300);
+        if (!(bn > 1e-13 * scale)) { st->steps = k + 1; st->stop = 2; }
+      }
+      st->ticket[3] = 0;
+    }
+  }
+}
+
+// ---- symmetric tridiagonal eigen-solver (one block) ----------------------------------------
+// Number of eigenvalues of T (alpha[0..m), beta[1..m)) below x: sign changes of the LDL^T
+// pivots, computed without divisions by rescaling a three-term recurrence.
+__device__ int sturm_count(const double* a, const double* b, int m, double x) {
+  // p_i = (a_i - x) p_{i-1} - b_i^2 p_{i-2}; count sign changes of p_i / p_{i-1}
+  // a zero p_i is replaced by a tiny value of the opposite sign of p_{i-1} (a tiny negative
+  // pivot), the usual convention for an eigenvalue exactly at x
+  double p0 = 1.0, p1 = a[0] - x;
+  if (p1 == 0.0) p1 = -0x1.0p-900;
+  int cnt = (p1 < 0.0) ? 1 : 0;
+  for (int i = 1; i < m; ++i) {
+    const double bb = b[i] * b[i];
+    double p2 = (a[i] - x) * p1 - bb * p0;
+    if (p2 == 0.0) p2 = -p1 * 0x1.0p-60;
+    if ((p2 < 0.0) != (p1 < 0.0)) ++cnt;
+    // rescale to avoid overflow/underflow (exact powers of two)
+    const double ap = fabs(p2);
+    if (ap > 0x1.0p+400 || ap < 0x1.0p-400) {
+      const int e = ilogb(ap);
+      p2 = scalbn(p2, -e);
+      p1 = scalbn(p1, -e);
+    }
+    p0 = p1;
+    p1 = p2;
+  }
+  return cnt;
+}
+
+// Lowest eigenvalue by 32-way multisection (warp 0 evaluates the Sturm counts; FP64 is a
+// scarce pipe on this GPU, so fewer points per round cost less in total), then optionally
+// the eigenvector by inverse iteration (thread 0, FP64, partial pivoting).
+constexpr int MS_PTS = 32;
+__device__ double tridiag_lowest_block(const double* a, const double* b, int m, double* vec, double* work) {
+  __shared__ double lo_s, hi_s;
+  __shared__ int cnt_s[MS_PTS];
+  if (threadIdx.x == 0) {
+    double lo = a[0], hi = a[0];
+    for (int i = 0; i < m; ++i) {
+      const double r = (i > 0 ? fabs(b[i]) : 0.0) + (i + 1 < m ? fabs(b[i + 1]) : 0.0);
+      lo = fmin(lo, a[i] - r);
+      hi = fmax(hi, a[i] + r);
+    }
+    const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
+    lo_s = lo - pad;
+    hi_s = hi + pad;
+  }
+  __syncthreads();
+  for (int round = 0; round < 16; ++round) {
+    const double lo = lo_s, hi = hi_s;
+    if (threadIdx.x < MS_PTS) {
+      const double x = lo + (hi - lo) * (double)(threadIdx.x + 1) / (double)(MS_PTS + 1);
+      cnt_s[threadIdx.x] = sturm_count(a, b, m, x);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      while (t < MS_PTS && cnt_s[t] == 0) ++t;  // first point with >=1 eigenvalue below
+      const double nlo = (t == 0) ? lo : lo + (hi - lo) * (double)t / (double)(MS_PTS + 1);
+      const double nhi = (t == MS_PTS) ? hi : lo + (hi - lo) * (double)(t + 1) / (double)(MS_PTS + 1);
+      lo_s = nlo;
+      hi_s = nhi;
+    }
+    __syncthreads();
+    if (hi_s - lo_s <= 4e-16 * fmax(fabs(lo_s), fabs(hi_s)) + 1e-300) break;
+  }
+  const double ev = 0.5 * (lo_s + hi_s);
+  if (vec && threadIdx.x == 0) {
+    // inverse iteration: (T - ev I) y = v, Gaussian elimination with partial pivoting.
+    // work: 5*m doubles (diag, super, super2, sub multipliers, pivot flags)
+    double* dd = work;           // diagonal of U
+    double* du = work + m;       // first super-diagonal of U
+    double* du2 = work + 2 * m;  // second super-diagonal of U
+    double* ml = work + 3 * m;   // multipliers
+    double* pv = work + 4 * m;   // 1.0 if rows swapped at step i
+    const double tiny = 1e-300 + 1e-15 * fmax(fabs(ev), 1.0) * 1e-3;
+    for (int i = 0; i < m; ++i) vec[i] = 1.0 / sqrt((double)m) * (1.0 + 0.01 * (double)((i * 7919) % 13) / 13.0);
+    for (int it = 0; it < 3; ++it) {
+      // factor T - ev I (rebuilt each iteration; m is small)
+      for (int i = 0; i < m; ++i) { dd[i] = a[i] - ev; du[i] = (i + 1 < m) ? b[i + 1] : 0.0; du2[i] = 0.0; }
+      for (int i = 0; i < m - 1; ++i) {
+        const double sub = b[i + 1];
+        if (fabs(dd[i]) >= fabs(sub)) {
+          pv[i] = 0.0;
+          if (dd[i] == 0.0) dd[i] = tiny;
+          const double l = sub / dd[i];
+          ml[i] = l;
+          dd[i + 1] -= l * du[i];
+        } else {
+          pv[i] = 1.0;
+          const double l = dd[i] / sub;
+          ml[i] = l;
+          // swap rows i and i+1
+          const double t0 = dd[i + 1], t1 = (i + 2 < m) ? du[i + 1] : 0.0;
+          dd[i] = sub;
+          const double odu = du[i];
+          du[i] = t0;
+          du2[i] = t1;
+          dd[i + 1] = odu - l * t0;
+          if (i + 2 < m) du[i + 1] = -l * t1;
+        }
+      }
+      if (dd[m - 1] == 0.0) dd[m - 1] = tiny;
+      // forward: apply L^-1 to vec
+      for (int i = 0; i < m - 1; ++i) {
+        if (pv[i] != 0.0) { const double t = vec[i]; vec[i] = vec[i + 1]; vec[i + 1] = t - ml[i] * vec[i]; }
+        else vec[i + 1] -= ml[i] * vec[i];
+      }
+      // back substitution
+      for (int i = m - 1; i >= 0; --i) {
+        double s = vec[i];
+        if (i + 1 < m) s -= du[i] * vec[i + 1];
+        if (i + 2 < m) s -= du2[i] * vec[i + 2];
+        vec[i] = s / dd[i];
+      }
+      double nrm = 0.0;
+      for (int i = 0; i < m; ++i) nrm = fma(vec[i], vec[i], nrm);
+      nrm = 1.0 / sqrt(nrm);
+      for (int i = 0; i < m; ++i) vec[i] *= nrm;
+    }
+    // sign convention: first nonzero component positive
+    double sg = 1.0;
+    for (int i = 0; i < m; ++i) if (vec[i] != 0.0) { sg = vec[i] > 0 ? 1.0 : -1.0; break; }
+    for (int i = 0; i < m; ++i) vec[i] *= sg;
+  }
+  __syncthreads();
+  return ev;
+}
+
+// convergence check after step k (T has size k+1): Ritz residual |beta_{k+1} * s_k| of the
+// lowest Ritz pair, relative to max(1, |E|)
+__global__ void k_lz_check(const double* alpha, const double* beta, int k, double tol, LzState* st, double* c,
+                           double* work) {
+  if (lz_stopped(st)) return;
+  const double e = tridiag_lowest_block(alpha, beta, k + 1, c, work);
+  if (threadIdx.x == 0) {
+    const double res = fabs(beta[k + 1] * c[k]);
+    if (res <= tol * fmax(1.0, fabs(e))) { st->stop = 1; st->steps = k + 1; }
+    st->e_prev = e;
+    st->energy = e;
+    st->residual = res;
+  }
+}
+
+// final eigenpair of T_m; m = st->steps if stopped else kmax
+__global__ void k_lz_final(const double* alpha, const double* beta, int kmax, LzState* st, double* c, double* work) {
+  const int m = st->stop ? st->steps : kmax;
+  const double e = tridiag_lowest_block(alpha, beta, m, c, work);
+  if (threadIdx.x == 0) {
+    st->energy = e;
+    st->steps = m;
+    st->residual = fabs(beta[m] * c[m - 1]);
+  }
+}
+
+__global__ void k_tridiag(const double* alpha, const double* beta, int m, double* value, double* vec, double* work) {
+  const double e = tridiag_lowest_block(alpha, beta, m, vec, work);
+  if (threadIdx.x == 0) *value = e;
+}
+
+// psi = sum_{k<m} c_k Q[k]
+__global__ void k_ritz(const double* __restrict__ Q, int64_t ldq, const double* __restrict__ c, const LzState* st,
+                       double* __restrict__ out, int64_t n) {
+  const int m = st->steps;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double x = 0.0;
+    for (int k = 0; k < m; ++k) x = fma(c[k], Q[(int64_t)k * ldq + i], x);
+    out[i] = x;
+  }
+}
+
+// ---- workspace layout ----------------------------------------------------------------------
+struct LzLayout {
+  int64_t nvec;      // vectors in the basis store
+  size_t off_basis, off_w, off_partial, off_h, off_c, off_work, off_state, off_scalars, total;
+  int nparts;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static LzLayout lz_layout(int64_t D, int K, bool store, int nparts) {
+  LzLayout L;
+  L.nparts = nparts;
+  L.nvec = store ? (int64_t)K + 1 : 3;
+  size_t o = 0;
+  L.off_basis = o; o = align256(o + (size_t)L.nvec * D * sizeof(double));
+  L.off_w = o; o = align256(o + (size_t)D * sizeof(double));
+  L.off_partial = o; o = align256(o + (size_t)nparts * (K + 2) * sizeof(double));
+  L.off_h = o; o = align256(o + (size_t)(K + 2) * sizeof(double));
+  L.off_c = o; o = align256(o + (size_t)(K + 2) * sizeof(double));
+  L.off_work = o; o = align256(o + (size_t)5 * (K + 2) * sizeof(double));
+  L.off_scalars = o; o = align256(o + 8 * sizeof(double));
+  L.off_state = o; o = align256(o + sizeof(LzState));
+  L.total = o;
+  return L;
+}
+
+static int lz_parts(const ed_plan_s* p, int64_t D) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>((D + LZ_NT - 1) / LZ_NT, (int64_t)p->ctx->num_sms * 4));
+}
+
+}  // namespace ed
+
+using namespace ed;
+
+extern "C" {
+
+ED_API ed_status ed_lanczos_workspace(ed_plan p, const ed_lanczos_params* prm, size_t* bytes) {
+  ED_TRY(check_plan(p));
+  if (!prm || !bytes) return fail(ED_ERR_INVALID_ARG, "null argument");
+  if (prm->max_steps < 1 || prm->max_steps > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  const bool store = prm->want_vector || prm->reorth;
+  *bytes = lz_layout(p->dim, prm->max_steps, store, lz_parts(p, p->dim)).total;
+  return ED_OK;
+}
+
+ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const double* d_v0, void* d_work, size_t work_bytes,
+                            double* d_alpha, double* d_beta, double* d_evec, ed_lanczos_result* res,
+                            ed_stream_t stream) {
+  ED_TRY(check_plan(p));
+  if (!prm || !res || !d_alpha || !d_beta) return fail(ED_ERR_INVALID_ARG, "null argument");
+  const int K = prm->max_steps;
+  if (K < 1 || K > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  const int64_t D = p->dim;
+  if (D < 1) return fail(ED_ERR_INVALID_ARG, "empty sector");
+  if (prm->want_vector && !d_evec) return fail(ED_ERR_INVALID_ARG, "want_vector needs d_evec");
+  const bool store = prm->want_vector || prm->reorth;
+  const int nparts = lz_parts(p, D);
+  const LzLayout L = lz_layout(D, K, store, nparts);
+  if (!d_work || work_bytes < L.total) return fail(ED_ERR_INVALID_ARG, "workspace too small (see ed_lanczos_workspace)");
+  if (prm->reorth && K + 1 > 1024) return fail(ED_ERR_INVALID_ARG, "reorth supports max_steps <= 1023");
+  cudaStream_t s = as_stream(stream);
+  char* base = (char*)d_work;
+  double* Q = (double*)(base + L.off_basis);
+  double* w = (double*)(base + L.off_w);
+  double* part = (double*)(base + L.off_partial);
+  double* h = (double*)(base + L.off_h);
+  double* c = (double*)(base + L.off_c);
+  double* twork = (double*)(base + L.off_work);
+  double* scal = (double*)(base + L.off_scalars);
+  LzState* st = (LzState*)(base + L.off_state);
+  ED_CUDA(cudaMemsetAsync(st, 0, sizeof(LzState), s));
+  ED_CUDA(cudaMemsetAsync(d_alpha, 0, K * sizeof(double), s));
+  ED_CUDA(cudaMemsetAsync(d_beta, 0, (K + 1) * sizeof(double), s));
+  {
+    // e_prev = +inf so the first check never converges
+    const double inf = INFINITY;
+    ED_CUDA(cudaMemcpyAsync(&st->e_prev, &inf, sizeof(double), cudaMemcpyHostToDevice, s));
+    ED_CUDA(cudaStreamSynchronize(s));
+  }
+  const int gv = nparts;
+  const int gs = grid_for(D, 256, p->ctx->num_sms * 8);
+  auto qv = [&](int k) -> double* { return Q + (int64_t)(store ? k : (k % 3)) * D; };
+  // q_0
+  if (d_v0) {
+    ED_CUDA(cudaMemcpyAsync(qv(0), d_v0, D * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  } else {
+    k_random_start<<<gs, 256, 0, s>>>(qv(0), D, prm->seed);
+    ED_CHECK_LAUNCH("k_random_start");
+  }
+  k_dot<<<gv, LZ_NT, 0, s>>>(qv(0), qv(0), D, part, st, 0, scal, scal + 1, nullptr);
+  k_scale<<<gs, 256, 0, s>>>(qv(0), qv(0), D, scal + 1, nullptr);
+  ED_CHECK_LAUNCH_N("lanczos start", 2);
+  {
+    double n2 = 0.0;
+    ED_CUDA(cudaMemcpyAsync(&n2, scal, sizeof(double), cudaMemcpyDeviceToHost, s));
+    ED_CUDA(cudaStreamSynchronize(s));
+    if (!std::isfinite(n2)) return fail(ED_ERR_NONFINITE, "start vector is not finite");
+    if (n2 == 0.0) return fail(ED_ERR_ZERO_VECTOR, "start vector has zero norm");
+  }
+  // optional per-matvec CUDA events on the launching stream
+  std::vector<cudaEvent_t> ev;
+  if (prm->profile) {
+    ev.resize(2 * (size_t)K);
+    for (auto& e : ev) ED_CUDA(cudaEventCreate(&e));
+  }
+  const int* stopf = &st->stop;
+  // the Krylov dimension cannot exceed D; without reorthogonalisation rounding would
+  // otherwise keep beta alive past it
+  const int Km = (int)std::min<int64_t>(K, D);
+  for (int k = 0; k < Km; ++k) {
+    double* q = qv(k);
+    double* qp = k > 0 ? qv(k - 1) : nullptr;
+    if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k], s));
+    ED_TRY(matvec_f64(p, q, w, 1, D, s, stopf));
+    if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k + 1], s));
+    k_dot<<<gv, LZ_NT, 0, s>>>(q, w, D, part, st, 0, d_alpha + k, nullptr, stopf);
+    const bool last_norm = !prm->reorth;
+    k_lz_update<<<gv, LZ_NT, 0, s>>>(w, q, qp, D, d_alpha + k, d_beta + k, part, st, d_beta + k + 1, k, last_norm);
+    uint64_t nl = 3;
+    if (prm->reorth) {
+      for (int pass = 0; pass < 2; ++pass) {
+        k_multidot<<<gv, LZ_NT, 0, s>>>(Q, D, k + 1, w, D, part, h, st);
+        k_multiaxpy<<<gv, LZ_NT, 0, s>>>(Q, D, k + 1, h, w, D, part, st, d_beta + k + 1, k, pass == 1, d_alpha + k);
+        nl += 2;
+      }
+    }
+    k_scale<<<gs, 256, 0, s>>>(w, qv(k + 1), D, d_beta + k + 1, stopf);
+    if (prm->check_every > 0 && ((k + 1) % prm->check_every == 0) && k + 1 < Km) {
+      k_lz_check<<<1, LZ_NT, 0, s>>>(d_alpha, d_beta, k, prm->tol, st, c, twork);
+      ++nl;
+    }
+    ED_CHECK_LAUNCH_N("lanczos step", nl);
+  }
+  k_lz_final<<<1, LZ_NT, 0, s>>>(d_alpha, d_beta, Km, st, c, twork);
+  ED_CHECK_LAUNCH("k_lz_final");
+  if (prm->want_vector) {
+    k_ritz<<<gs, 256, 0, s>>>(Q, D, c, st, d_evec, D);
+    k_dot<<<gv, LZ_NT, 0, s>>>(d_evec, d_evec, D, part, st, 0, scal, scal + 1, nullptr);
+    k_scale<<<gs, 256, 0, s>>>(d_evec, d_evec, D, scal + 1, nullptr);
+    ED_CHECK_LAUNCH_N("lanczos ritz", 3);
+  }
+  LzState hs;
+  ED_CUDA(cudaMemcpyAsync(&hs, st, sizeof(LzState), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  res->energy = hs.energy;
+  res->residual = hs.residual;
+  res->steps = hs.steps;
+  res->converged = hs.stop;
+  res->status = hs.status;
+  res->matvec_ms = 0.0;
+  res->matvecs = 0;
+  if (prm->profile) {
+    // matvecs after a stop return immediately; count only the steps that ran
+    for (int k = 0; k < hs.steps; ++k) {
+      float ms = 0.f;
+      ED_CUDA(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));
+      res->matvec_ms += ms;
+      res->matvecs += 1;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+  }
+  return ED_OK;
+}
+
+ED_API ed_status ed_lanczos_coeffs(ed_plan p, int K, const double* d_start, void* d_work, size_t work_bytes,
+                                   double* d_alpha, double* d_beta, int* h_steps, double* h_norm, ed_stream_t stream) {
+  ED_TRY(check_plan(p));
+  if (!d_start || !d_alpha || !d_beta || !h_steps || !h_norm) return fail(ED_ERR_INVALID_ARG, "null argument");
+  if (K < 1 || K > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  const int64_t D = p->dim;
+  if (D < 1) return fail(ED_ERR_INVALID_ARG, "empty sector");
+  const int nparts = lz_parts(p, D);
+  const LzLayout L = lz_layout(D, K, false, nparts);
+  if (!d_work || work_bytes < L.total) return fail(ED_ERR_INVALID_ARG, "workspace too small (see ed_lanczos_workspace)");
+  cudaStream_t s = as_stream(stream);
+  char* base = (char*)d_work;
+  double* Q = (double*)(base + L.off_basis);
+  double* w = (double*)(base + L.off_w);
+  double* part = (double*)(base + L.off_partial);
+  double* scal = (double*)(base + L.off_scalars);
+  LzState* st = (LzState*)(base + L.off_state);
+  ED_CUDA(cudaMemsetAsync(st, 0, sizeof(LzState), s));
+  ED_CUDA(cudaMemsetAsync(d_alpha, 0, K * sizeof(double), s));
+  ED_CUDA(cudaMemsetAsync(d_beta, 0, (K + 1) * sizeof(double), s));
+  const int gv = nparts;
+  const int gs = grid_for(D, 256, p->ctx->num_sms * 8);
+  auto qv = [&](int k) -> double* { return Q + (int64_t)(k % 3) * D; };
+  k_dot<<<gv, LZ_NT, 0, s>>>(d_start, d_start, D, part, st, 0, scal, scal + 1, nullptr);
+  k_scale<<<gs, 256, 0, s>>>(d_start, qv(0), D, scal + 1, nullptr);
+  ED_CHECK_LAUNCH_N("lanczos_coeffs start", 2);
+  double n2 = 0.0;
+  ED_CUDA(cudaMemcpyAsync(&n2, scal, sizeof(double), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  if (!std::isfinite(n2)) return fail(ED_ERR_NONFINITE, "start vector is not finite");
+  if (n2 == 0.0) { *h_steps = 0; *h_norm = 0.0; return ED_OK; }
+  const int* stopf = &st->stop;
+  const int Km = (int)std::min<int64_t>(K, D);
+  for (int k = 0; k < Km; ++k) {
+    double* q = qv(k);
+    double* qp = k > 0 ? qv(k - 1) : nullptr;
+    ED_TRY(matvec_f64(p, q, w, 1, D, s, stopf));
+    k_dot<<<gv, LZ_NT, 0, s>>>(q, w, D, part, st, 0, d_alpha + k, nullptr, stopf);
+    k_lz_update<<<gv, LZ_NT, 0, s>>>(w, q, qp, D, d_alpha + k, d_beta + k, part, st, d_beta + k + 1, k, 1);
+    k_scale<<<gs, 256, 0, s>>>(w, qv(k + 1), D, d_beta + k + 1, stopf);
+    ED_CHECK_LAUNCH_N("lanczos_coeffs step", 3);
+  }
+  LzState hs;
+  ED_CUDA(cudaMemcpyAsync(&hs, st, sizeof(LzState), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  *h_steps = hs.stop ? hs.steps : Km;
+  *h_norm = std::sqrt(n2);
+  return ED_OK;
+}
+
+ED_API ed_status ed_tridiag_lowest(const double* d_alpha, const double* d_beta, int m, double* d_value, double* d_vec,
+                                   ed_stream_t stream) {
+  if (m < 1 || m > 4096) return fail(ED_ERR_INVALID_ARG, "m must be in [1, 4096]");
+  if (!d_alpha || !d_beta || !d_value) return fail(ED_ERR_INVALID_ARG, "null argument");
+  cudaStream_t s = as_stream(stream);
+  double* work = nullptr;
+  if (d_vec) ED_CUDA(cudaMallocAsync(&work, 5 * (size_t)m * sizeof(double), s));
+  k_tridiag<<<1, LZ_NT, 0, s>>>(d_alpha, d_beta, m, d_value, d_vec, work);
+  ED_CHECK_LAUNCH("k_tridiag");
+  if (work) ED_CUDA(cudaFreeAsync(work, s));
+  return ED_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,353 @@
+"""Exact-diagonalisation drivers — drop-in for ``cmpy.exactdiag`` (cmpy/exactdiag.py).
+
+* ``compute_groundstate`` (exactdiag.py:24-43): every (n_up, n_dn) sector, dense eigh for
+  dim <= thresh, otherwise the device Lanczos (replacing ARPACK ``eigsh``).
+* ``solve_sector`` / ``gf_lehmann`` / ``GreensFunctionMeasurement`` (exactdiag.py:46-245):
+  thermal Lehmann sum with dense sector eigenproblems, the c^dag application, overlaps and
+  the pole sum all on the GPU.
+* ``gf_continued_fraction``: zero-temperature G(z) from Lanczos coefficients of c^dag|gs>
+  and c|gs> (no reference counterpart; the reference's dense Lanczos helpers are
+  exactdiag.py:324-375, mirrored below on the device).
+"""
+
+from __future__ import annotations
+
+import logging
+from typing import NamedTuple, Optional
+
+import numpy as np
+import torch
+
+from . import engine as E
+from .basis import DN, UP, Sector
+from .models import AbstractManyBodyModel
+
+logger = logging.getLogger("cmpy_gb300")
+
+__all__ = [
+    "EigenState",
+    "compute_groundstate",
+    "solve_sector",
+    "occupation_up",
+    "occupation_dn",
+    "occupation",
+    "double_occupation",
+    "accumulate_gf",
+    "GreensFunctionMeasurement",
+    "gf_lehmann",
+    "gf_lehmann_zero_temperature",
+    "gf_continued_fraction",
+    "iter_lanczos_coeffs",
+    "lanczos_coeffs",
+    "lanczos_matrix",
+    "lanczos_ground_state",
+]
+
+
+class EigenState(NamedTuple):
+    """Ground-state record (cmpy/matrix.py:42-47)."""
+
+    energy: float = np.inf
+    state: np.ndarray = None
+    n_up: int = None
+    n_dn: int = None
+
+
+def _dense_eigh(plan: E.Plan):
+    H = plan.dense()
+    w, v = torch.linalg.eigh(H)
+    return w, v
+
+
+def _sector_plan(model, n_up, n_dn) -> E.Plan:
+    return model.plan(n_up, n_dn)
+
+
+def groundstate_sector(model, n_up: int, n_dn: int, thresh: int = 50, max_steps: int = 400,
+                       tol: float = 1e-12, check_every: int = 10):
+    """(energy, device ground-state vector) of one sector."""
+    plan = _sector_plan(model, n_up, n_dn)
+    D = plan.dim
+    if D <= thresh:
+        w, v = _dense_eigh(plan)
+        i = int(torch.argmin(w).item())
+        return float(w[i].item()), v[:, i].contiguous()
+    res = E.lanczos(plan, max_steps=min(max_steps, D), want_vector=True, tol=tol, check_every=check_every)
+    return res.energy, res.vector
+
+
+def compute_groundstate(model, thresh: int = 50, max_steps: int = 400, tol: float = 1e-12) -> EigenState:
+    """Lowest eigenstate over all sectors (cmpy/exactdiag.py:24-43)."""
+    gs = EigenState()
+    best_vec = None
+    for n_up, n_dn in model.basis.iter_fillings():
+        energy, vec = groundstate_sector(model, n_up, n_dn, thresh, max_steps, tol)
+        logger.debug("Sector (%d, %d): E0 = %.12f", n_up, n_dn, energy)
+        if energy < gs.energy:
+            gs = EigenState(energy, None, n_up, n_dn)
+            best_vec = vec
+    if best_vec is not None:
+        gs = gs._replace(state=best_vec.cpu().numpy())
+    return gs
+
+
+def _solve_sector_dev(model, sector: Sector, cache: dict = None):
+    key = (sector.n_up, sector.n_dn)
+    if cache is not None and key in cache:
+        w, v = cache[key]
+        return E._as_dev_f64(w), E._as_dev_f64(v)
+    w, v = _dense_eigh(_sector_plan(model, sector.n_up, sector.n_dn))
+    if cache is not None:
+        cache[key] = [w, v]
+    return w, v
+
+
+def solve_sector(model: AbstractManyBodyModel, sector: Sector, cache: dict = None):
+    """Dense eigenpairs of one sector (cmpy/exactdiag.py:46-57), computed on the GPU."""
+    w, v = _solve_sector_dev(model, sector, cache)
+    return w.cpu().numpy(), v.cpu().numpy()
+
+
+# -- thermal observables (cmpy/exactdiag.py:60-107), on the device --------------------------
+
+
+def _state_masks(up_states, dn_states):
+    dev = E.device()
+    up = torch.as_tensor(np.asarray(up_states, dtype=np.int64)).to(dev)
+    dn = torch.as_tensor(np.asarray(dn_states, dtype=np.int64)).to(dev)
+    return up, dn
+
+
+def _weights(evals, beta, emin):
+    return torch.exp(-beta * (E._as_dev_f64(evals) - emin))
+
+
+def occupation_up(up_states, dn_states, evals, evecs, beta, emin, pos):
+    up, dn = _state_masks(up_states, dn_states)
+    V = E._as_dev_f64(evecs).reshape(len(up), len(dn), -1)
+    sel = ((up >> pos) & 1).bool()
+    overlap = (V[sel] ** 2).sum(dim=(0, 1))
+    return float((_weights(evals, beta, emin) * overlap).sum().item())
+
+
+def occupation_dn(up_states, dn_states, evals, evecs, beta, emin, pos):
+    up, dn = _state_masks(up_states, dn_states)
+    V = E._as_dev_f64(evecs).reshape(len(up), len(dn), -1)
+    sel = ((dn >> pos) & 1).bool()
+    overlap = (V[:, sel] ** 2).sum(dim=(0, 1))
+    return float((_weights(evals, beta, emin) * overlap).sum().item())
+
+
+def occupation(up_states, dn_states, evals, evecs, beta, emin=0.0, pos=0, sigma=UP):
+    if sigma == UP:
+        return occupation_up(up_states, dn_states, evals, evecs, beta, emin, pos)
+    return occupation_dn(up_states, dn_states, evals, evecs, beta, emin, pos)
+
+
+def double_occupation(up_states, dn_states, evals, evecs, beta, emin, pos):
+    up, dn = _state_masks(up_states, dn_states)
+    V = E._as_dev_f64(evecs).reshape(len(up), len(dn), -1)
+    both = (((up[:, None] & dn[None, :]) >> pos) & 1).bool()
+    overlap = (V[both] ** 2).sum(dim=0)
+    return float((_weights(evals, beta, emin) * overlap).sum().item())
+
+
+def accumulate_gf(gf, z, cdag, evals, evecs, evals_p1, evecs_p1, beta, emin=0.0):
+    """gf += Lehmann poles of one sector pair (cmpy/exactdiag.py:110-134). `cdag` is a
+    CreationOperator (its device map is used); `gf` is a complex128 torch CUDA tensor."""
+    V = E._as_dev_f64(evecs)
+    Vp = E._as_dev_f64(evecs_p1)
+    CV = cdag._apply_dev(V)
+    ov = (Vp.t() @ CV) ** 2
+    return E.lehmann_accumulate(evals, evals_p1, ov, float(beta), float(emin), z, gf)
+
+
+class GreensFunctionMeasurement:
+    """Running thermal Lehmann accumulation (cmpy/exactdiag.py:137-212)."""
+
+    def __init__(self, z, beta, pos=0, sigma=UP, dtype=None, measure_occ=True):
+        self.z = z
+        self.beta = beta
+        self.pos = pos
+        self.sigma = sigma
+        self._measure_occ = measure_occ
+        self._zt = E._as_dev_c128(z)
+        self._part = 0.0
+        self._gs_energy = np.inf
+        self._gf = torch.zeros_like(self._zt)
+        self._occ = 0.0
+        self._occ_double = 0.0
+
+    @property
+    def part(self):
+        return self._part * np.exp(-self.beta * self._gs_energy)
+
+    @property
+    def gf(self):
+        g = (self._gf / self._part).cpu().numpy()
+        return g.reshape(np.shape(self.z)) if np.ndim(self.z) else g
+
+    @property
+    def occ(self):
+        return self._occ / self._part
+
+    @property
+    def occ_double(self):
+        return self._occ_double / self._part
+
+    @property
+    def gs_energy(self):
+        return self._gs_energy
+
+    def accumulate(self, sector, sector_p1, evals, evecs, evals_p1, evecs_p1, cdag):
+        evals_t = E._as_dev_f64(evals)
+        min_energy = float(evals_t.min().item())
+        factor = 1.0
+        if min_energy < self._gs_energy:
+            factor = float(np.exp(-self.beta * (self._gs_energy - min_energy)))
+            self._gs_energy = min_energy
+        e0 = self._gs_energy
+        self._part = self._part * factor + float(torch.exp(-self.beta * (evals_t - e0)).sum().item())
+        if factor != 1.0:
+            self._gf *= factor
+        accumulate_gf(self._gf, self._zt, cdag, evals_t, evecs, evals_p1, evecs_p1, self.beta, e0)
+        if self._measure_occ:
+            up, dn = sector.up_states, sector.dn_states
+            self._occ = self._occ * factor + occupation(up, dn, evals_t, evecs, self.beta, e0, self.pos, self.sigma)
+            self._occ_double = self._occ_double * factor + double_occupation(up, dn, evals_t, evecs, self.beta, e0,
+                                                                             self.pos)
+
+
+def gf_lehmann(model, z, beta, pos=0, sigma=UP, eig_cache=None, occ=True, jw_sign: bool = False):
+    """Thermal Lehmann Green's function over all sectors (cmpy/exactdiag.py:215-245)."""
+    from .operators import CreationOperator
+
+    basis = model.basis
+    data = GreensFunctionMeasurement(z, beta, pos, sigma, measure_occ=occ)
+    eig_cache = eig_cache if eig_cache is not None else dict()
+    for n_up, n_dn in basis.iter_fillings():
+        sector = model.get_sector(n_up, n_dn)
+        sector_p1 = basis.upper_sector(n_up, n_dn, sigma)
+        if sector_p1 is None:
+            continue
+        w, v = _solve_sector_dev(model, sector, eig_cache)
+        wp, vp = _solve_sector_dev(model, sector_p1, eig_cache)
+        cdag = CreationOperator(sector, sector_p1, pos=pos, sigma=sigma, jw_sign=jw_sign)
+        data.accumulate(sector, sector_p1, w, v, wp, vp, cdag)
+    return data
+
+
+def _neighbour(model, n_up, n_dn, sigma, delta):
+    nu, nd = (n_up + delta, n_dn) if sigma == UP else (n_up, n_dn + delta)
+    if not (0 <= nu <= model.num_sites and 0 <= nd <= model.num_sites):
+        return None
+    return nu, nd
+
+
+def gf_lehmann_zero_temperature(model, z, gs_energy: float, gs_state, n_up: int, n_dn: int, pos=0, sigma=UP,
+                                jw_sign: bool = False) -> np.ndarray:
+    """T=0 Lehmann G(z) of a non-degenerate ground state from the dense eigenpairs of the two
+    neighbouring sectors: sum_m |<m|c^dag|0>|^2/(z-E_m+E0) + sum_n |<n|c|0>|^2/(z+E_n-E0)."""
+    plan = _sector_plan(model, n_up, n_dn)
+    psi = E._as_dev_f64(gs_state).reshape(-1)
+    zt = E._as_dev_c128(z)
+    g = torch.zeros_like(zt)
+    e0 = torch.tensor([gs_energy], dtype=torch.float64, device=E.device())
+    for delta, create in ((1, True), (-1, False)):
+        nb = _neighbour(model, n_up, n_dn, sigma, delta)
+        if nb is None:
+            continue
+        tplan = _sector_plan(model, *nb)
+        phi = plan.apply_fermion(tplan, pos, sigma, create, psi, jw_sign=jw_sign)
+        w, v = _dense_eigh(tplan)
+        amp = (v.t() @ phi) ** 2  # |<m|phi>|^2
+        if create:  # poles at E_m - E0, weights amp (Lehmann with unit ground-state weight)
+            E.lehmann_accumulate(e0, w, amp.reshape(-1, 1), float("inf"), 0.0, zt, g)
+        else:  # poles at E0 - E_n:  1/(z - (E0 - E_n))
+            E.lehmann_accumulate(w, e0, amp.reshape(1, -1), float("inf"), 0.0, zt, g)
+    # unit weights (beta=inf) add w_n + w'_m = 2 per pole; undo that factor
+    return (g / 2).cpu().numpy()
+
+
+def gf_continued_fraction(model, z, n_up: int, n_dn: int, gs_energy: float, gs_state, pos=0, sigma=UP,
+                          n_lev: int = 200, jw_sign: bool = False, return_coeffs: bool = False):
+    """T=0 G(z) = <0|c (z-H+E0)^-1 c^dag|0> + <0|c^dag (z+H-E0)^-1 c|0> from the Lanczos
+    continued fractions of c^dag|0> and c|0>, evaluated on the device for every z."""
+    plan = _sector_plan(model, n_up, n_dn)
+    psi = E._as_dev_f64(gs_state).reshape(-1)
+    zt = E._as_dev_c128(z)
+    g = torch.zeros_like(zt)
+    coeffs = {}
+    for delta, create, sign in ((1, True, 1), (-1, False, -1)):
+        nb = _neighbour(model, n_up, n_dn, sigma, delta)
+        if nb is None:
+            continue
+        tplan = _sector_plan(model, *nb)
+        phi = plan.apply_fermion(tplan, pos, sigma, create, psi, jw_sign=jw_sign)
+        a, b, nrm = E.lanczos_coeffs(tplan, phi, max_steps=min(n_lev, tplan.dim))
+        coeffs["particle" if create else "hole"] = (a, b, nrm)
+        if a.numel() == 0:
+            continue
+        E.continued_fraction(a, b, nrm * nrm, zt, e0=gs_energy, sign=sign, out=g)
+    out = g.cpu().numpy()
+    return (out, coeffs) if return_coeffs else out
+
+
+# -- Lanczos helpers (cmpy/exactdiag.py:324-375) on the device ------------------------------
+
+
+def _as_operator_dev(ham):
+    from .operators import HamiltonOperator
+
+    if isinstance(ham, HamiltonOperator):
+        return ham._apply_dev
+    H = E._as_dev_f64(ham)
+    return lambda x: H @ x
+
+
+def iter_lanczos_coeffs(ham, size=10, seed: Optional[int] = None):
+    """Un-normalised Lanczos (a_n, b_n) with a uniform(0,1) start, no reorthogonalisation
+    (cmpy/exactdiag.py:324-347), on the device."""
+    apply = _as_operator_dev(ham)
+    n = ham.shape[0]
+    g = torch.Generator(device="cpu")
+    if seed is not None:
+        g.manual_seed(int(seed))
+    psi = torch.rand(n, generator=g, dtype=torch.float64).to(E.device())
+    hpsi = apply(psi)
+    a = torch.dot(psi, hpsi) / torch.dot(psi, psi)
+    yield float(a.item()), None
+    psi_prev, psi = psi, hpsi - a * psi
+    for _ in range(1, size):
+        hpsi = apply(psi)
+        pp = torch.dot(psi, psi)
+        a = torch.dot(psi, hpsi) / pp
+        b2 = pp / torch.dot(psi_prev, psi_prev)
+        psi_new = hpsi - a * psi - b2 * psi_prev
+        yield float(a.item()), float(torch.sqrt(b2).item())
+        psi_prev, psi = psi, psi_new
+
+
+def lanczos_coeffs(ham, size=10, seed: Optional[int] = None):
+    a_coeffs, b_coeffs = [], []
+    for a, b in iter_lanczos_coeffs(ham, size, seed):
+        a_coeffs.append(a)
+        b_coeffs.append(b)
+    b_coeffs.pop(0)
+    return a_coeffs, b_coeffs
+
+
+def lanczos_matrix(a_coeffs, b_coeffs):
+    mat = np.diag(a_coeffs)
+    np.fill_diagonal(mat[1:], b_coeffs)
+    np.fill_diagonal(mat[:, 1:], b_coeffs)
+    return mat
+
+
+def lanczos_ground_state(a_coeffs, b_coeffs, max_eig=3):
+    """Lowest eigenpair of the Lanczos tridiagonal matrix, solved on the device
+    (cmpy/exactdiag.py:368-375)."""
+    a = np.asarray(a_coeffs, dtype=np.float64)
+    b = np.concatenate([[0.0], np.asarray(b_coeffs, dtype=np.float64)])
+    e, v = E.tridiag_lowest(a, b, want_vector=True)
+    return e, v.cpu().numpy()

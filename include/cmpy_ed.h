@@ -1,0 +1,293 @@
+/*
+ * cmpy_ed.h — C ABI of the GB300 exact-diagonalisation engine (libcmpy_ed.so).
+ *
+ * The engine replaces the hot path of cmpy: Fock-sector enumeration (cmpy/basis.py),
+ * the COO Hamiltonian projectors (cmpy/operators.py), the HamiltonOperator matvec
+ * (cmpy/operators.py:614-646), the fermionic creation/annihilation operators
+ * (cmpy/operators.py:652-791), the ground-state driver (cmpy/exactdiag.py:24-57) and the
+ * Green's functions (cmpy/exactdiag.py:110-245).
+ *
+ * Conventions (identical to the reference):
+ *   - site i <-> bit i of a uint64 bitstring (LSB = site 0);
+ *   - a spin sector lists the ascending integers with popcount n (colex order), so the
+ *     index of a state is rank(s) = sum_k C(p_k, k) over its set-bit positions p_1<p_2<...;
+ *   - many-body index is up-major: idx = up_idx * num_dn + dn_idx;
+ *   - values are IEEE FP64, indices int64.
+ *
+ * Memory: every vector/array argument prefixed d_ is caller-owned DEVICE memory; h_ is
+ * host memory. Plans (opaque) own only their small per-spin tables. Every call is
+ * asynchronous on the given stream unless its comment says "synchronous", and returns an
+ * ed_status; nothing throws. A plan is not thread-safe; separate plans are.
+ */
+#ifndef CMPY_ED_H
+#define CMPY_ED_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define ED_API __attribute__((visibility("default")))
+#else
+#define ED_API
+#endif
+
+typedef void* ed_stream_t; /* a cudaStream_t; NULL = legacy default stream */
+
+typedef enum ed_status {
+  ED_OK = 0,
+  ED_ERR_INVALID_ARG = 1,  /* bad size/pointer/site index (reference: assert / ValueError) */
+  ED_ERR_CUDA = 2,         /* a CUDA runtime call failed; see ed_last_error() */
+  ED_ERR_TIMEOUT = 3,      /* a bounded device-side wait ran out */
+  ED_ERR_NONFINITE = 4,    /* NaN/Inf in model parameters or start vector */
+  ED_ERR_TOO_LARGE = 5,    /* dimension beyond the engine's index range / capacity */
+  ED_ERR_ZERO_VECTOR = 6,  /* start vector has zero norm */
+  ED_ERR_DEVICE = 7,       /* a kernel's own bounds check fired (device status word) */
+  ED_ERR_NOT_FOUND = 8     /* target sector does not exist (e.g. c^dag on a full sector) */
+} ed_status;
+
+/* ---- library ------------------------------------------------------------------------ */
+
+ED_API const char* ed_status_string(int status);
+/* Last error message of the calling thread (CUDA error string or argument diagnostic). */
+ED_API const char* ed_last_error(void);
+ED_API int ed_version(void); /* major*10000 + minor*100 + patch */
+/* Number of kernels this library has launched in the process (all devices, all threads). */
+ED_API uint64_t ed_launch_count(void);
+
+/* ---- basis: cmpy/basis.py ----------------------------------------------------------- */
+
+/* Binomial coefficient C(n, k) for 0 <= k <= n <= 63 (else 0). Host function. */
+ED_API int64_t ed_binomial(int n, int k);
+
+/* Number of states of a spin sector: C(n_sites, n), or 2^n_sites when n < 0 ("n=None"). */
+ED_API int64_t ed_sector_size(int n_sites, int n);
+
+/* Replaces Basis.generate_states / get_states (cmpy/basis.py:655-676) and the
+ * init_sectors scan (cmpy/basis.py:644-653): writes the ascending states with popcount
+ * n into d_out[0 .. ed_sector_size(n_sites, n)). n < 0 writes 0 .. 2^n_sites - 1.
+ * n_sites <= 62. capacity is the length of d_out in elements. */
+ED_API ed_status ed_enumerate(int n_sites, int n, uint64_t* d_out, int64_t capacity,
+                              ed_stream_t stream);
+
+/* Index of each state inside its own popcount sector (the combinatorial number system);
+ * equals bisect_left(get_states(popcount(s)), s) (cmpy/operators.py:276-299). */
+ED_API ed_status ed_rank(const uint64_t* d_states, int64_t count, int64_t* d_ranks,
+                         ed_stream_t stream);
+
+/* ---- models: cmpy/models/hubbard.py, anderson.py, heisenberg.py --------------------- */
+
+/* Fermionic model descriptor (host memory, copied at plan creation).
+ *   eps[i]  on-site energy of site i, chemical potential already subtracted
+ *           (HubbardModel: eps - mu, cmpy/models/hubbard.py:77;
+ *            SIAM: [eps_imp - mu, eps_bath...], cmpy/models/anderson.py:151);
+ *   u[i]    Hubbard U of site i (SIAM: [U, 0, ...], cmpy/models/anderson.py:150);
+ *   bonds   (site1 < site2, hop) in emission order (hubbard.py:19-21 keeps i<j pairs of
+ *           the neighbour list; anderson.py:156-158 has (0, j+1, v_j));
+ *   sign_width  the `width` of the reference's fermionic sign bit_count
+ *           (cmpy/operators.py:253-273,425-433): n_sites for HubbardModel, 0 for the SIAM
+ *           (cmpy/models/anderson.py:149 passes nsites = 0, i.e. no sign). */
+typedef struct ed_fermion_model {
+  int32_t n_sites;
+  int32_t n_bonds;
+  int32_t sign_width;
+  int32_t reserved;
+  const double* h_eps;
+  const double* h_u;
+  const int32_t* h_bond_site1;
+  const int32_t* h_bond_site2;
+  const double* h_bond_hop;
+} ed_fermion_model;
+
+/* Spin-1/2 XXZ model on directed site pairs, in the emission order of
+ * HeisenbergModel._hamiltonian_data (cmpy/models/heisenberg.py:19-40): for every state,
+ * for pos1 in 0..n_sites-1, for pos2 in neighbours(pos1). Each pair carries its own
+ * coupling (the reference has one uniform j, jz; per-pair values generalise it). Per
+ * directed pair the diagonal gets sign*0.25*jz and a flip gets (0.25*j)/2. */
+typedef struct ed_spin_model {
+  int32_t n_sites;
+  int32_t n_pairs;
+  const int32_t* h_pos1;
+  const int32_t* h_pos2;
+  const double* h_j;
+  const double* h_jz;
+} ed_spin_model;
+
+/* ---- plans: one Hamiltonian sector on one device ------------------------------------- */
+
+typedef struct ed_plan_s* ed_plan;
+
+typedef struct ed_plan_info {
+  int64_t dim;        /* sector dimension D */
+  int64_t num_up;     /* number of up states (spin model: D) */
+  int64_t num_dn;     /* number of dn states (spin model: 1) */
+  int64_t hop_up;     /* single-spin hopping table entries, up */
+  int64_t hop_dn;     /* single-spin hopping table entries, dn */
+  int64_t nnz;        /* triplets the reference generator would emit for this sector */
+  int32_t n_sites;
+  int32_t kind;       /* 0 fermion, 1 spin */
+  int32_t n_up;
+  int32_t n_dn;
+  double hnorm_bound; /* upper bound of ||H||_inf (max row abs sum) */
+} ed_plan_info;
+
+/* Build the sector basis and hopping tables on the device (replaces
+ * AbstractManyBodyModel.hamilton_operator's setup, cmpy/models/abc.py:250-256).
+ * n_up/n_dn in 0..n_sites. Synchronous on `stream` (it reads back table sizes). */
+ED_API ed_status ed_plan_create_fermion(const ed_fermion_model* model, int n_up, int n_dn,
+                                        ed_plan* out, ed_stream_t stream);
+/* Spin model: sector with n_up up-spins (AbstractSpinModel.hamilton_operator,
+ * cmpy/models/abc.py:194-199; SpinBasis.get_states(s) with n_up = N/2 + s). */
+ED_API ed_status ed_plan_create_spin(const ed_spin_model* model, int n_up, ed_plan* out,
+                                     ed_stream_t stream);
+ED_API ed_status ed_plan_destroy(ed_plan plan);
+ED_API ed_status ed_plan_get_info(ed_plan plan, ed_plan_info* out);
+/* Device pointers to the plan's sorted spin-sector states (valid until destroy). */
+ED_API ed_status ed_plan_states(ed_plan plan, const uint64_t** d_up, const uint64_t** d_dn);
+
+/* ---- Hamiltonian application: HamiltonOperator._matvec (cmpy/operators.py:626-630) --- */
+
+/* y = H x for the plan's sector (H is real symmetric, so this equals the reference's
+ * y[col] += val * x[row] loop over its triplets). d_x, d_y: FP64[D], must not alias. */
+ED_API ed_status ed_matvec(ed_plan plan, const double* d_x, double* d_y, ed_stream_t stream);
+/* Y = H X for n_vec column-major vectors with leading dimension ld >= D
+ * (LinearOperator._matmat). */
+ED_API ed_status ed_matmat(ed_plan plan, const double* d_x, double* d_y, int64_t n_vec,
+                           int64_t ld, ed_stream_t stream);
+/* Dense H (row-major D x D) for small sectors, summed in triplet order like
+ * HamiltonOperator.toarray (cmpy/operators.py:632-635). D <= 32768. */
+ED_API ed_status ed_dense(ed_plan plan, double* d_out, ed_stream_t stream);
+/* Diagonal of H (HamiltonOperator._trace sums it, cmpy/operators.py:641-646). */
+ED_API ed_status ed_diagonal(ed_plan plan, double* d_out, ed_stream_t stream);
+
+/* Generic sparse operator for user-supplied triplets (HamiltonOperator(size, data, indices),
+ * cmpy/operators.py:617-630): y[r] = sum_k vals[k] * x[cols[k]] over k in
+ * [rowptr[r], rowptr[r+1]), accumulated in storage order from 0.0 with separately rounded
+ * multiply and add. Storing the triplets transposed and stably sorted by their column
+ * reproduces the reference loop `y[col] += val * x[row]` bit for bit. */
+ED_API ed_status ed_csr_matvec(int64_t n_rows, const int64_t* d_rowptr, const int64_t* d_cols,
+                               const double* d_vals, const double* d_x, double* d_y,
+                               ed_stream_t stream);
+
+/* ---- COO projectors: cmpy/operators.py:305-527, hubbard.py:13-22, heisenberg.py:19-40 */
+
+/* Triplet segments in the reference's emission order. Each function works in two calls:
+ * with d_rows == NULL it only counts (synchronous; *h_nnz receives the count), otherwise it
+ * writes exactly that many triplets into d_rows/d_cols/d_vals (capacity elements). The
+ * state arrays may be any ascending list (bisect_left semantics are kept exactly). */
+
+/* project_onsite_energy(up_states, dn_states, eps) — cmpy/operators.py:359-422 */
+ED_API ed_status ed_coo_onsite(const uint64_t* d_up, int64_t num_up, const uint64_t* d_dn,
+                               int64_t num_dn, const double* h_eps, int n_values,
+                               int64_t* d_rows, int64_t* d_cols, double* d_vals,
+                               int64_t capacity, int64_t* h_nnz, ed_stream_t stream);
+/* project_hubbard_inter(up_states, dn_states, u) — cmpy/operators.py:305-356 */
+ED_API ed_status ed_coo_inter(const uint64_t* d_up, int64_t num_up, const uint64_t* d_dn,
+                              int64_t num_dn, const double* h_u, int n_values,
+                              int64_t* d_rows, int64_t* d_cols, double* d_vals,
+                              int64_t capacity, int64_t* h_nnz, ed_stream_t stream);
+/* project_hopping(up_states, dn_states, num_sites, site1, site2, hop) —
+ * cmpy/operators.py:463-527 (width = num_sites for the sign). site1 < site2. */
+ED_API ed_status ed_coo_hopping(const uint64_t* d_up, int64_t num_up, const uint64_t* d_dn,
+                                int64_t num_dn, int width, int site1, int site2, double hop,
+                                int64_t* d_rows, int64_t* d_cols, double* d_vals,
+                                int64_t capacity, int64_t* h_nnz, ed_stream_t stream);
+/* Whole model, the concatenation _ham_data emits (hubbard.py:13-22 / anderson.py:147-158
+ * / heisenberg.py:19-40) for the plan's sector. */
+ED_API ed_status ed_coo_plan(ed_plan plan, int64_t* d_rows, int64_t* d_cols, double* d_vals,
+                             int64_t capacity, int64_t* h_nnz, ed_stream_t stream);
+
+/* ---- fermion operators: cmpy/operators.py:652-791 ------------------------------------ */
+
+/* y = c^dag_{pos,sigma} x (create=1) or c_{pos,sigma} x (create=0), from the plan's sector
+ * to the plan_target sector (n_sigma +/- 1). jw_sign=0 reproduces the reference (no
+ * Jordan-Wigner sign, cmpy/operators.py:652-703); jw_sign=1 applies the fermionic sign
+ * (-1)^(number of same-spin electrons below pos, plus all up electrons for sigma=dn).
+ * sigma: 1 = up, 2 = dn (cmpy/basis.py:39). d_y is fully written (zeros where no source).
+ * Applies to n_vec column vectors (leading dimensions ld_x >= D, ld_y >= D_target), the
+ * matmat of CreationOperator.matmat(evecs) in cmpy/exactdiag.py:132-134. */
+ED_API ed_status ed_apply_fermion(ed_plan plan, ed_plan plan_target, int pos, int sigma,
+                                  int create, int jw_sign, const double* d_x, double* d_y,
+                                  int64_t n_vec, int64_t ld_x, int64_t ld_y,
+                                  ed_stream_t stream);
+
+/* ---- Lanczos ground state (replaces eigsh in cmpy/exactdiag.py:24-43) ----------------- */
+
+typedef struct ed_lanczos_params {
+  int32_t max_steps;     /* Krylov dimension limit K */
+  int32_t reorth;        /* 0 = none (plain three-term), 1 = full (classical Gram-Schmidt twice) */
+  int32_t check_every;   /* device-side convergence test period (0 = never, run K steps) */
+  int32_t want_vector;   /* 1 = form the Ritz ground-state vector (needs the stored basis) */
+  double tol;            /* stop when the Ritz residual |beta_m s_m| <= tol * max(1, |E|) */
+  uint64_t seed;         /* start vector seed when d_v0 == NULL */
+  int32_t profile;       /* 1 = time every matvec launch with CUDA events on `stream` */
+  int32_t reserved;
+} ed_lanczos_params;
+
+typedef struct ed_lanczos_result {
+  double energy;         /* lowest Ritz value */
+  double residual;       /* |beta_m * s_m| Ritz residual estimate */
+  double matvec_ms;      /* total matvec kernel time (profile = 1), else 0 */
+  int32_t steps;         /* Lanczos steps taken (size m of T) */
+  int32_t converged;     /* 1 if tol met, 2 if invariant subspace (breakdown) */
+  int32_t status;        /* device status word */
+  int32_t matvecs;       /* matvec launches timed */
+} ed_lanczos_result;
+
+/* Bytes of caller-provided device workspace for ed_lanczos (Krylov basis included). */
+ED_API ed_status ed_lanczos_workspace(ed_plan plan, const ed_lanczos_params* params,
+                                      size_t* h_bytes);
+/* Runs the Lanczos iteration on the device. d_v0: optional start vector FP64[D].
+ * Writes alpha[0..steps) and beta[0..steps] (beta[0] = 0, beta[k] couples k-1 and k,
+ * beta[steps] is the residual coupling) into d_alpha (FP64[max_steps]) and d_beta
+ * (FP64[max_steps+1]), the normalised ground state to d_evec (FP64[D], if want_vector).
+ * Synchronous at the end (fills *h_result). */
+ED_API ed_status ed_lanczos(ed_plan plan, const ed_lanczos_params* params,
+                            const double* d_v0, void* d_work, size_t work_bytes,
+                            double* d_alpha, double* d_beta, double* d_evec,
+                            ed_lanczos_result* h_result, ed_stream_t stream);
+
+/* Lanczos coefficients of the Krylov space of d_start (not normalised; its norm is
+ * returned in *h_norm): the continued-fraction input of the Green's function. No basis is
+ * stored (three vectors of workspace). Returns the number of steps in *h_steps. */
+ED_API ed_status ed_lanczos_coeffs(ed_plan plan, int max_steps, const double* d_start,
+                                   void* d_work, size_t work_bytes, double* d_alpha,
+                                   double* d_beta, int* h_steps, double* h_norm,
+                                   ed_stream_t stream);
+
+/* Lowest eigenpair of the symmetric tridiagonal matrix (alpha[0..m), beta[1..m)) on the
+ * device, FP64 (replaces scipy.linalg.eigh_tridiagonal in cmpy/exactdiag.py:368-375).
+ * d_vec (FP64[m]) may be NULL. */
+ED_API ed_status ed_tridiag_lowest(const double* d_alpha, const double* d_beta, int m,
+                                   double* d_value, double* d_vec, ed_stream_t stream);
+
+/* ---- Green's functions -------------------------------------------------------------- */
+
+/* Continued fraction G(z) = sign * norm2 / (z' - a0 - b1^2 / (z' - a1 - ...)) with
+ * z' = sign * z + shift over n_z complex frequencies (interleaved re,im FP64), adding into
+ * d_g when accumulate=1. With E0 the ground-state energy and (a, b, norm2) the Lanczos
+ * coefficients of c^dag|gs> (resp. c|gs>): electron part sign=+1, shift=E0; hole part
+ * sign=-1, shift=E0. */
+ED_API ed_status ed_gf_continued_fraction(const double* d_alpha, const double* d_beta,
+                                          int n_lev, double norm2, double shift, int sign,
+                                          const double* d_z, int64_t n_z, double* d_g,
+                                          int accumulate, ed_stream_t stream);
+
+/* Lehmann pole sum of cmpy/exactdiag.py:110-129 (_accumulate_sum): with the overlap
+ * matrix ov[m, n] = |<m|c^dag|n>|^2 (FP64, d_p1 x d, row-major), adds
+ *   sum_{m,n} ov[m,n] (w_n + w'_m) / (z - E'_m + E_n),  w = exp(-beta (E - emin))
+ * to g[z] (interleaved complex FP64). beta = +inf gives unit weights like the reference. */
+ED_API ed_status ed_lehmann_accumulate(const double* d_evals, int64_t n_d,
+                                       const double* d_evals_p1, int64_t n_dp1,
+                                       const double* d_overlap, double beta, double emin,
+                                       const double* d_z, int64_t n_z, double* d_g,
+                                       ed_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CMPY_ED_H */
