@@ -86,7 +86,7 @@ class LanczosParams(C.Structure):
         ("tol", C.c_double),
         ("seed", C.c_uint64),
         ("profile", C.c_int32),
-        ("reserved", C.c_int32),
+        ("arithmetic", C.c_int32),
     ]
 
 
@@ -140,6 +140,22 @@ _SIGNATURES = {
     ),
     "ed_lanczos_coeffs": (I32, [PLAN, I32, P, P, C.c_size_t, P, P, C.POINTER(I32), C.POINTER(F64), P]),
     "ed_tridiag_lowest": (I32, [P, P, I32, P, P, P]),
+    "ed_batch_create": (I32, [C.POINTER(C.c_void_p), I32, C.POINTER(C.c_void_p)]),
+    "ed_batch_destroy": (I32, [C.c_void_p]),
+    "ed_batch_workspace": (I32, [C.c_void_p, I32, I32, I32, C.POINTER(C.c_size_t)]),
+    "ed_batch_lanczos": (
+        I32,
+        [C.c_void_p, I32, F64, I32, C.c_uint64, P, I32, P, C.c_size_t, P, P, P, P, P, P, P, I32, I32, P],
+    ),
+    "ed_batch_tune": (
+        I32,
+        [C.c_void_p, I32, P, C.c_size_t, P, P, P, P, P, C.POINTER(I32), C.POINTER(I32), C.POINTER(C.c_float), P],
+    ),
+    "ed_batch_gf_continued_fraction": (I32, [I32, I32, P, P, P, P, I32, P, I64, P, P]),
+    "ed_plan_fixed_point": (I32, [PLAN]),
+    "ed_fixed_from_f64": (I32, [P, I64, I32, P, C.POINTER(C.c_int32), P]),
+    "ed_fixed_to_f64": (I32, [P, I64, C.c_int32, P, P]),
+    "ed_matvec_fixed": (I32, [PLAN, P, C.c_int32, P, C.POINTER(C.c_int32), C.POINTER(I32), P]),
     "ed_gf_continued_fraction": (I32, [P, P, I32, F64, F64, I32, P, I64, P, I32, P]),
     "ed_lehmann_accumulate": (I32, [P, I64, P, I64, P, F64, F64, P, I64, P, P]),
 }

@@ -1,0 +1,920 @@
+// Block-fixed-point (BFP) Lanczos for fermionic sectors with one hopping magnitude.
+//
+// Why: on GB300 the FP64 pipe issues ~1.6 operations per clock per SM (measured), about 60x
+// fewer than INT32 adds, while a Hubbard matvec needs ~16 FP64 operations per 16 bytes of
+// HBM traffic — an FP64 matvec would run at <10% of HBM bandwidth. Here a Lanczos vector is
+// stored as int64 mantissas with one power-of-two exponent per vector (value = m * 2^e):
+//   * matvec: W = diag_int * X + t_int * sum(+-X_nbr) — exact int64 arithmetic;
+//   * alpha, norms: exact 128-bit integer dot products, reduced to FP64 per thread;
+//   * three-term update: 128-bit fixed-point products with one rounding per element;
+//   * FP64 only for the scalars (alpha, beta, the tridiagonal solve).
+// The vector stored for step k is the unnormalised residual r_k (||r_k|| = beta_k), so the
+// normalisation 1/beta_k is folded into the scalar coefficients and needs no pass of its own.
+// Per Lanczos step: one matvec kernel (+ alpha) and one update kernel (+ norm) — 48 B/element.
+//
+// Reductions are deterministic (fixed grid, per-block partials, last-block sum in block order).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <vector>
+
+#include "ed_plan.cuh"
+#include "ed_tridiag.cuh"
+
+namespace ed {
+
+// ---- 128-bit helpers ------------------------------------------------------------------------
+struct I128 {
+  uint64_t lo;
+  int64_t hi;
+};
+
+__device__ __forceinline__ I128 mul_s64(int64_t a, int64_t b) {
+  I128 r;
+  r.lo = (uint64_t)a * (uint64_t)b;
+  r.hi = __mul64hi(a, b);
+  return r;
+}
+
+__device__ __forceinline__ void add128(I128& acc, const I128& v) {
+  asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, %3;"
+      : "+l"(acc.lo), "+l"(acc.hi)
+      : "l"(v.lo), "l"(v.hi));
+}
+
+__device__ __forceinline__ double i128_to_double(const I128& v) {
+  return fma((double)v.hi, 0x1.0p64, (double)v.lo);
+}
+
+// round-to-nearest arithmetic right shift of a 128-bit value by 1 <= s <= 63, result in int64
+__device__ __forceinline__ int64_t shr128_round(I128 v, int s) {
+  I128 h;
+  h.lo = 1ull << (s - 1);
+  h.hi = 0;
+  add128(v, h);
+  return (int64_t)((v.lo >> s) | ((uint64_t)v.hi << (64 - s)));
+}
+
+__device__ __forceinline__ unsigned long long uabs64(int64_t v) {
+  return v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+}
+
+// ---- shared per-solve state --------------------------------------------------------------------
+struct BfpState {
+  int stop;            // 0 running, 1 converged, 2 invariant subspace
+  int steps;
+  int status;
+  int pad;
+  // update coefficients for the current step (written by the matvec's last block)
+  int64_t A_w, A_q, A_p;
+  int SA;
+  int ew;              // exponent of W
+  unsigned long long maxw;
+  double energy, residual, e_prev;
+  unsigned int ticket[4];
+};
+
+struct BfpVecs {
+  int64_t* R;          // vectors, slot stride D
+  int32_t* eR;         // exponent per Lanczos index
+  unsigned long long* maxR;  // max |mantissa| per Lanczos index
+  int store;           // 1: slot k = index k; 0: ring of 3
+  int64_t D;
+  __host__ __device__ __forceinline__ int64_t* vec(int k) const { return R + (int64_t)(store ? k : (k % 3)) * D; }
+};
+
+constexpr int BT = 256;  // block size of the streaming kernels
+
+template <int NT>
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v, unsigned long long* sm) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sm[w] = v;
+  __syncthreads();
+  unsigned long long r = 0;
+  if (w == 0) {
+    r = (l < NT / 32) ? sm[l] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r = max(r, __shfl_xor_sync(0xffffffffu, r, o));
+  }
+  return r;
+}
+
+__device__ __forceinline__ bool bfp_last_block(unsigned int* ticket) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (am_last) __threadfence();
+  return am_last;
+}
+
+// ---- conversion FP64 <-> BFP ------------------------------------------------------------------
+__global__ void k_maxabs_f64(const double* __restrict__ x, int64_t n, unsigned long long* out) {
+  __shared__ unsigned long long sm[BT / 32];
+  unsigned long long m = 0;
+  for (int64_t i = blockIdx.x * (int64_t)BT + threadIdx.x; i < n; i += (int64_t)gridDim.x * BT) {
+    const double v = x[i];
+    unsigned long long b = (unsigned long long)__double_as_longlong(fabs(v));
+    if (!isfinite(v)) b = 0x7FF0000000000000ull;
+    m = max(m, b);
+  }
+  m = block_max_u64<BT>(m, sm);
+  if (threadIdx.x == 0) atomicMax(out, m);
+}
+
+// xm = round(x * 2^-e) with e chosen so that max|xm| < 2^m_in
+__global__ void k_f64_to_bfp(const double* __restrict__ x, int64_t n, const unsigned long long* maxbits, int m_in,
+                             int64_t* __restrict__ xm, int32_t* e_out, unsigned long long* max_out) {
+  const double mx = __longlong_as_double((long long)*maxbits);
+  int e2 = 0;
+  frexp(mx, &e2);  // mx < 2^e2
+  const int e = e2 - m_in;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *e_out = e;
+    *max_out = (unsigned long long)llrint(ldexp(mx, -e));
+  }
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    xm[i] = llrint(ldexp(x[i], -e));
+}
+
+__global__ void k_bfp_to_f64(const int64_t* __restrict__ xm, const int32_t* e, int64_t n, double* __restrict__ x) {
+  const int ee = *e;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = ldexp((double)xm[i], ee);
+}
+
+// ||R||^2 (exact per thread) -> beta[k]; also used for the start vector
+__global__ void k_bfp_norm(BfpVecs v, int k, double* partial, BfpState* st, double* beta) {
+  __shared__ double sm[BT / 32];
+  const int64_t* x = v.vec(k);
+  I128 acc{0, 0};
+  for (int64_t i = blockIdx.x * (int64_t)BT + threadIdx.x; i < v.D; i += (int64_t)gridDim.x * BT)
+    add128(acc, mul_s64(x[i], x[i]));
+  double s = block_sum<BT>(i128_to_double(acc), sm);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (bfp_last_block(&st->ticket[0])) {
+    double t = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += BT) t += ((volatile double*)partial)[b];
+    t = block_sum<BT>(t, sm);
+    if (threadIdx.x == 0) {
+      beta[k] = ldexp(sqrt(t), v.eR[k]);
+      st->ticket[0] = 0;
+    }
+  }
+}
+
+// ---- the matvec ----------------------------------------------------------------------------------
+struct BfpHubArgs {
+  int64_t nu, nd;
+  const int32_t* up_off; const int32_t* up_npos; const int32_t* up_idx;
+  const uint16_t* dn_tab; int max_dn;
+  const uint64_t* up_states; const uint64_t* dn_states;
+  const int32_t* e_up; const int32_t* e_dn;
+  int u_uniform; int32_t u0; int32_t u[ED_MAX_SITES + 2];
+  int32_t t_int; int F;
+  // diagonal mode 1 (arbitrary FP64 energies): int64 fixed point, shift = Fd - F
+  const int64_t* e_up_fx; const int64_t* e_dn_fx;
+  int64_t u0_fx; int64_t u_fx[ED_MAX_SITES + 2];
+  int dshift;
+};
+
+__device__ __forceinline__ int32_t bfp_uterm(const BfpHubArgs& a, uint64_t both) {
+  if (a.u_uniform) return a.u0 * __popcll(both);
+  int32_t v = 0;
+  while (both) {
+    v += a.u[__ffsll((long long)both) - 1];
+    both &= both - 1;
+  }
+  return v;
+}
+
+__device__ __forceinline__ int64_t bfp_uterm64(const BfpHubArgs& a, uint64_t both) {
+  if (a.u_uniform) return a.u0_fx * (int64_t)__popcll(both);
+  int64_t v = 0;
+  while (both) {
+    v += a.u_fx[__ffsll((long long)both) - 1];
+    both &= both - 1;
+  }
+  return v;
+}
+
+// diagonal term D(x) of one element in units of the output grid
+template <bool DIAG64>
+__device__ __forceinline__ int64_t bfp_diag_term(const BfpHubArgs& a, int64_t row_e32, int64_t row_e64,
+                                                 uint64_t su, int64_t d, int64_t x) {
+  const uint64_t both = su & __ldg(a.dn_states + d);
+  if (!DIAG64) {
+    const int32_t dg = (int32_t)row_e32 + __ldg(a.e_dn + d) + bfp_uterm(a, both);
+    return (int64_t)dg * x;
+  } else {
+    const int64_t dg = row_e64 + __ldg(a.e_dn_fx + d) + bfp_uterm64(a, both);
+    return shr128_round(mul_s64(dg, x), a.dshift);
+  }
+}
+
+// One CTA per target up-row (grid-stride). The row is staged in shared memory with its
+// negation (dn-hop gathers pick the signed slot), up-neighbour rows stream from global.
+// Epilogue: exact alpha partial <X, W> and max|W|. When x_scale != null the kernel is the
+// public ed_matvec_fixed (no Lanczos scalars).
+template <int NT, bool VEC2, bool DIAG64>
+__global__ void __launch_bounds__(NT) k_bfp_hub_matvec(BfpHubArgs a, const int64_t* __restrict__ X,
+                                                      int64_t* __restrict__ W, double* partial,
+                                                      unsigned long long* partial_max, BfpState* st) {
+  if (st && *(volatile int*)&st->stop) return;
+  extern __shared__ int64_t xs[];  // [2*nd + 1]
+  __shared__ double smd[NT / 32];
+  __shared__ unsigned long long smu[NT / 32];
+  const int64_t nd = a.nd;
+  if (threadIdx.x == 0) xs[2 * nd] = 0;
+  I128 dot{0, 0};
+  unsigned long long mx = 0;
+  for (int64_t row = blockIdx.x; row < a.nu; row += gridDim.x) {
+    const int64_t* xrow = X + row * nd;
+    for (int64_t d = threadIdx.x; d < nd; d += NT) {
+      const int64_t v = __ldg(xrow + d);
+      xs[d] = v;
+      xs[nd + d] = -v;
+    }
+    __syncthreads();
+    const int32_t o0 = __ldg(a.up_off + row), o1 = __ldg(a.up_off + row + 1);
+    const int32_t op = o0 + __ldg(a.up_npos + row);
+    const uint64_t su = __ldg(a.up_states + row);
+    const int64_t eu = DIAG64 ? 0 : (int64_t)__ldg(a.e_up + row);
+    const int64_t eu64 = DIAG64 ? __ldg(a.e_up_fx + row) : 0;
+    if (VEC2) {
+      for (int64_t d = 2 * threadIdx.x; d < nd; d += 2 * NT) {
+        int64_t h0 = 0, h1 = 0;
+        for (int32_t e = o0; e < op; ++e) {
+          const longlong2 v = __ldg((const longlong2*)(X + (int64_t)__ldg(a.up_idx + e) * nd + d));
+          h0 += v.x;
+          h1 += v.y;
+        }
+        for (int32_t e = op; e < o1; ++e) {
+          const longlong2 v = __ldg((const longlong2*)(X + (int64_t)__ldg(a.up_idx + e) * nd + d));
+          h0 -= v.x;
+          h1 -= v.y;
+        }
+        const uint32_t* tab = (const uint32_t*)a.dn_tab;
+        for (int e = 0; e < a.max_dn; ++e) {
+          const uint32_t sl = __ldg(tab + ((int64_t)e * nd + d) / 2);
+          h0 += xs[sl & 0xFFFFu];
+          h1 += xs[sl >> 16];
+        }
+        const int64_t x0 = xs[d], x1 = xs[d + 1];
+        const int64_t w0 = (int64_t)a.t_int * h0 + bfp_diag_term<DIAG64>(a, eu, eu64, su, d, x0);
+        const int64_t w1 = (int64_t)a.t_int * h1 + bfp_diag_term<DIAG64>(a, eu, eu64, su, d + 1, x1);
+        *(longlong2*)(W + row * nd + d) = make_longlong2(w0, w1);
+        add128(dot, mul_s64(x0, w0));
+        add128(dot, mul_s64(x1, w1));
+        mx = max(mx, max(uabs64(w0), uabs64(w1)));
+      }
+    } else {
+      for (int64_t d = threadIdx.x; d < nd; d += NT) {
+        int64_t h = 0;
+        for (int32_t e = o0; e < op; ++e) h += __ldg(X + (int64_t)__ldg(a.up_idx + e) * nd + d);
+        for (int32_t e = op; e < o1; ++e) h -= __ldg(X + (int64_t)__ldg(a.up_idx + e) * nd + d);
+        for (int e = 0; e < a.max_dn; ++e) h += xs[__ldg(a.dn_tab + (int64_t)e * nd + d)];
+        const int64_t x0 = xs[d];
+        const int64_t w0 = (int64_t)a.t_int * h + bfp_diag_term<DIAG64>(a, eu, eu64, su, d, x0);
+        W[row * nd + d] = w0;
+        add128(dot, mul_s64(x0, w0));
+        mx = max(mx, uabs64(w0));
+      }
+    }
+    __syncthreads();
+  }
+  if (!partial) return;
+  const double s = block_sum<NT>(i128_to_double(dot), smd);
+  const unsigned long long m = block_max_u64<NT>(mx, smu);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = s;
+    partial_max[blockIdx.x] = m;
+  }
+}
+
+// Lanczos scalars after the matvec of step k (single block, runs after the matvec):
+//   alpha_k = <R_k, W> / beta_k^2 ;  R_{k+1} = c_w W + c_q R_k + c_p R_{k-1}
+//   c_w = 1/beta_k, c_q = -alpha_k/beta_k, c_p = -beta_k/beta_{k-1}
+__global__ void k_bfp_scalars(BfpVecs v, int k, int F, int m_in, const double* partial,
+                              const unsigned long long* partial_max, int nparts, double* alpha, const double* beta,
+                              BfpState* st) {
+  if (*(volatile int*)&st->stop) return;
+  __shared__ double sm[BT / 32];
+  __shared__ unsigned long long smu[BT / 32];
+  double t = 0.0;
+  unsigned long long m = 0;
+  for (int b = threadIdx.x; b < nparts; b += BT) {
+    t += partial[b];
+    m = max(m, partial_max[b]);
+  }
+  t = block_sum<BT>(t, sm);
+  m = block_max_u64<BT>(m, smu);
+  if (threadIdx.x != 0) return;
+  const int ek = v.eR[k];
+  const int ew = ek - F;
+  const double bk = beta[k];
+  const double a = ldexp(t, ek + ew) / (bk * bk);
+  alpha[k] = a;
+  const double cw = 1.0 / bk, cq = -a / bk;
+  const double cp = (k > 0) ? -bk / beta[k - 1] : 0.0;
+  const int ep = (k > 0) ? v.eR[k - 1] : 0;
+  const double mw = (double)m, mq = (double)v.maxR[k], mp = (k > 0) ? (double)v.maxR[k - 1] : 0.0;
+  const double B = fabs(cw) * ldexp(mw, ew) + fabs(cq) * ldexp(mq, ek) + fabs(cp) * ldexp(mp, ep);
+  int eb = 0;
+  frexp(B > 0.0 ? B : 1.0, &eb);
+  const int er = eb - m_in;  // B * 2^-er < 2^m_in
+  const double gw = ldexp(cw, ew - er), gq = ldexp(cq, ek - er), gp = ldexp(cp, ep - er);
+  const double gm = fmax(fabs(gw), fmax(fabs(gq), fabs(gp)));
+  int eg = 0;
+  frexp(gm > 0.0 ? gm : 1.0, &eg);  // gm < 2^eg
+  const int SA = min(60, 60 - eg);
+  st->A_w = llrint(ldexp(gw, SA));
+  st->A_q = llrint(ldexp(gq, SA));
+  st->A_p = llrint(ldexp(gp, SA));
+  st->SA = SA;
+  st->ew = ew;
+  st->maxw = m;
+  v.eR[k + 1] = er;
+}
+
+// R_{k+1} = round((A_w W + A_q R_k + A_p R_{k-1}) / 2^SA); ||R_{k+1}||^2 and max -> beta[k+1]
+__global__ void k_bfp_update(BfpVecs v, int k, const int64_t* __restrict__ W, double* partial,
+                             unsigned long long* partial_max, double* beta, const double* alpha, BfpState* st,
+                             int final_k) {
+  if (*(volatile int*)&st->stop) return;
+  __shared__ double sm[BT / 32];
+  __shared__ unsigned long long smu[BT / 32];
+  const int64_t Aw = st->A_w, Aq = st->A_q, Ap = st->A_p;
+  const int SA = st->SA;
+  const int64_t* __restrict__ rq = v.vec(k);
+  const int64_t* __restrict__ rp = k > 0 ? v.vec(k - 1) : nullptr;
+  int64_t* __restrict__ rn = v.vec(k + 1);
+  I128 nrm{0, 0};
+  unsigned long long mx = 0;
+  for (int64_t i = blockIdx.x * (int64_t)BT + threadIdx.x; i < v.D; i += (int64_t)gridDim.x * BT) {
+    I128 s = mul_s64(Aw, W[i]);
+    add128(s, mul_s64(Aq, rq[i]));
+    if (rp) add128(s, mul_s64(Ap, rp[i]));
+    const int64_t r = shr128_round(s, SA);
+    rn[i] = r;
+    add128(nrm, mul_s64(r, r));
+    mx = max(mx, uabs64(r));
+  }
+  const double s = block_sum<BT>(i128_to_double(nrm), sm);
+  const unsigned long long m = block_max_u64<BT>(mx, smu);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = s;
+    partial_max[blockIdx.x] = m;
+  }
+  if (bfp_last_block(&st->ticket[1])) {
+    double t = 0.0;
+    unsigned long long mm = 0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += BT) {
+      t += ((volatile double*)partial)[b];
+      mm = max(mm, ((volatile unsigned long long*)partial_max)[b]);
+    }
+    t = block_sum<BT>(t, sm);
+    mm = block_max_u64<BT>(mm, smu);
+    if (threadIdx.x == 0) {
+      const double bn = ldexp(sqrt(t), v.eR[k + 1]);
+      beta[k + 1] = bn;
+      v.maxR[k + 1] = mm;
+      // invariant subspace: the new residual vanishes relative to the scale of T
+      // (beta[0] holds the start-vector norm, not an entry of T)
+      const double scale = fabs(alpha[k]) + (k > 0 ? beta[k] : 0.0) + 1e-300;
+      if (!(bn > 1e-13 * scale) || mm == 0) {
+        st->steps = k + 1;
+        st->stop = 2;
+      }
+      (void)final_k;
+      st->ticket[1] = 0;
+    }
+  }
+}
+
+// ---- Ritz vector ------------------------------------------------------------------------------------
+// C_k = round(c_k / beta_k * 2^(e_k + SC)) with one SC for all k; psi = sum_k C_k R_k * 2^-SC
+__global__ void k_bfp_ritz_coeffs(const BfpVecs v, const double* c, const double* beta, const BfpState* st,
+                                  int64_t* C, int* SC_out) {
+  if (threadIdx.x != 0) return;
+  const int m = st->steps;
+  double gm = 0.0;
+  for (int k = 0; k < m; ++k) gm = fmax(gm, fabs(ldexp(c[k] / beta[k], v.eR[k])));
+  int eg = 0;
+  frexp(gm > 0.0 ? gm : 1.0, &eg);
+  // |C_k| < 2^62 - 10 bits of headroom for the sum over k
+  const int SC = 52 - eg;
+  for (int k = 0; k < m; ++k) C[k] = llrint(ldexp(c[k] / beta[k], v.eR[k] + SC));
+  *SC_out = SC;
+}
+
+__global__ void k_bfp_ritz(const BfpVecs v, const int64_t* __restrict__ C, const int* SCp, const BfpState* st,
+                           double* __restrict__ out) {
+  const int m = st->steps;
+  const int SC = *SCp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < v.D; i += (int64_t)gridDim.x * blockDim.x) {
+    I128 acc{0, 0};
+    for (int k = 0; k < m; ++k) add128(acc, mul_s64(C[k], v.vec(k)[i]));
+    out[i] = ldexp(i128_to_double(acc), -SC);
+  }
+}
+
+// ---- tables ---------------------------------------------------------------------------------------------
+
+static bool is_int_scaled(double v, int F, int64_t lim) {
+  const double s = std::ldexp(v, F);
+  return std::isfinite(s) && s == std::floor(s) && std::fabs(s) < (double)lim;
+}
+
+ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
+  BfpTables& B = p->bfp;
+  B = BfpTables();
+  if (p->kind != 0 || p->dim == 0) return ED_OK;
+  // one hopping magnitude
+  double tmag = 0.0;
+  for (double h : p->hop) {
+    if (h == 0.0) continue;
+    if (tmag == 0.0) tmag = std::fabs(h);
+    else if (std::fabs(h) != tmag) return ED_OK;
+  }
+  if (p->num_dn * 2 + 1 > 65535) return ED_OK;  // 16-bit shared-memory slots
+  if ((2 * p->num_dn + 1) * 8 > 200 * 1024) return ED_OK;
+  // coefficients: per-state energies (exact FP64 sums), U and t as integers * 2^-F
+  std::vector<double> eu(p->num_up), edn(p->num_dn);
+  ED_CUDA(cudaMemcpyAsync(eu.data(), p->up.energy, p->num_up * sizeof(double), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(edn.data(), p->dn.energy, p->num_dn * sizeof(double), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  // mode 0: t, U and the state energies are integers * 2^-F (exact diagonal)
+  int F = -1;
+  for (int f = 0; f <= 40 && F < 0; ++f) {
+    bool ok = is_int_scaled(tmag, f, 1 << 24);
+    for (double v : p->u) ok = ok && is_int_scaled(v, f, 1 << 24);
+    for (double v : eu) ok = ok && is_int_scaled(v, f, 1 << 28);
+    for (double v : edn) ok = ok && is_int_scaled(v, f, 1 << 28);
+    if (ok) F = f;
+  }
+  int diag64 = 0;
+  if (F < 0) {
+    // mode 1: only t needs to be dyadic; the diagonal is an int64 fixed-point product
+    for (int f = 0; f <= 40 && F < 0; ++f)
+      if (is_int_scaled(tmag, f, 1 << 24)) F = f;
+    if (F < 0) return ED_OK;
+    diag64 = 1;
+  }
+  // row tables (host copies of the FP64 tables)
+  std::vector<int32_t> uoff(p->num_up + 1), uidx(p->up.nnz), doff(p->num_dn + 1), didx(p->dn.nnz);
+  std::vector<double> ucoef(p->up.nnz), dcoef(p->dn.nnz);
+  ED_CUDA(cudaMemcpyAsync(uoff.data(), p->up.off, uoff.size() * 4, cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(doff.data(), p->dn.off, doff.size() * 4, cudaMemcpyDeviceToHost, s));
+  if (p->up.nnz) {
+    ED_CUDA(cudaMemcpyAsync(uidx.data(), p->up.idx, uidx.size() * 4, cudaMemcpyDeviceToHost, s));
+    ED_CUDA(cudaMemcpyAsync(ucoef.data(), p->up.coef, ucoef.size() * 8, cudaMemcpyDeviceToHost, s));
+  }
+  if (p->dn.nnz) {
+    ED_CUDA(cudaMemcpyAsync(didx.data(), p->dn.idx, didx.size() * 4, cudaMemcpyDeviceToHost, s));
+    ED_CUDA(cudaMemcpyAsync(dcoef.data(), p->dn.coef, dcoef.size() * 8, cudaMemcpyDeviceToHost, s));
+  }
+  ED_CUDA(cudaStreamSynchronize(s));
+  const int64_t nu = p->num_up, nd = p->num_dn;
+  std::vector<int32_t> boff(nu + 1), bnpos(nu), bidx;
+  bidx.reserve(p->up.nnz);
+  int max_up = 0;
+  for (int64_t r = 0; r < nu; ++r) {
+    boff[r] = (int32_t)bidx.size();
+    int npos = 0;
+    for (int32_t k = uoff[r]; k < uoff[r + 1]; ++k)
+      if (ucoef[k] > 0.0) { bidx.push_back(uidx[k]); ++npos; }
+    for (int32_t k = uoff[r]; k < uoff[r + 1]; ++k)
+      if (ucoef[k] < 0.0) bidx.push_back(uidx[k]);
+    bnpos[r] = npos;
+    max_up = std::max(max_up, (int)(bidx.size() - boff[r]));
+  }
+  boff[nu] = (int32_t)bidx.size();
+  int max_dn = 0;
+  for (int64_t c = 0; c < nd; ++c) {
+    int n = 0;
+    for (int32_t k = doff[c]; k < doff[c + 1]; ++k) n += (dcoef[k] != 0.0);
+    max_dn = std::max(max_dn, n);
+  }
+  std::vector<uint16_t> tab((size_t)std::max(max_dn, 1) * nd, (uint16_t)(2 * nd));
+  for (int64_t c = 0; c < nd; ++c) {
+    int e = 0;
+    for (int32_t k = doff[c]; k < doff[c + 1]; ++k) {
+      if (dcoef[k] == 0.0) continue;
+      tab[(size_t)e * nd + c] = (uint16_t)(dcoef[k] > 0.0 ? didx[k] : nd + didx[k]);
+      ++e;
+    }
+  }
+  // diagonal bound in units of 2^-F, and the overflow guard
+  //   |W| <= (max|diag| 2^F + hops * t_int) * 2^m_in < 2^62
+  B.u_uniform = p->fp.u_uniform;
+  double max_eu = 0.0, max_ed = 0.0;
+  for (double v : eu) max_eu = std::max(max_eu, std::fabs(v));
+  for (double v : edn) max_ed = std::max(max_ed, std::fabs(v));
+  std::vector<double> uabs;
+  for (int i = 0; i < p->n_sites; ++i) uabs.push_back(std::fabs(p->u[i]));
+  std::sort(uabs.rbegin(), uabs.rend());
+  double usum = 0.0;
+  for (int i = 0; i < std::min(p->n_up, p->n_dn) && i < (int)uabs.size(); ++i) usum += uabs[i];
+  const double diag_max = max_eu + max_ed + usum;
+  B.t_int = (int32_t)std::ldexp(tmag, F);
+  const double bound = std::ldexp(diag_max, F) + (double)(max_up + max_dn) * B.t_int;
+  int lb = 0;
+  while (std::ldexp(1.0, lb) <= bound) ++lb;  // bound < 2^lb
+  const int m_in = std::min(56, 62 - lb);
+  if (m_in < 48) return ED_OK;
+  std::vector<int32_t> eui, edi;
+  std::vector<int64_t> euf, edf;
+  if (!diag64) {
+    eui.resize(nu);
+    edi.resize(nd);
+    for (int64_t i = 0; i < nu; ++i) eui[i] = (int32_t)std::ldexp(eu[i], F);
+    for (int64_t i = 0; i < nd; ++i) edi[i] = (int32_t)std::ldexp(edn[i], F);
+    for (int i = 0; i < p->n_sites; ++i) B.u_int[i] = (int32_t)std::ldexp(p->u[i], F);
+    B.u0_int = p->n_sites ? B.u_int[0] : 0;
+  } else {
+    // diag_fx = diag * 2^Fd with |diag_fx| < 2^61; the product with X (<= 2^m_in) is 128-bit
+    int ld = 0;
+    while (std::ldexp(1.0, ld) <= diag_max) ++ld;
+    B.Fd = 61 - ld;
+    if (B.Fd - F < 1 || B.Fd - F > 63) return ED_OK;
+    euf.resize(nu);
+    edf.resize(nd);
+    for (int64_t i = 0; i < nu; ++i) euf[i] = std::llrint(std::ldexp(eu[i], B.Fd));
+    for (int64_t i = 0; i < nd; ++i) edf[i] = std::llrint(std::ldexp(edn[i], B.Fd));
+    for (int i = 0; i < p->n_sites; ++i) B.u_fx[i] = std::llrint(std::ldexp(p->u[i], B.Fd));
+    B.u0_fx = p->n_sites ? B.u_fx[0] : 0;
+  }
+  B.diag64 = diag64;
+  B.F = F;
+  B.m_in = m_in;
+  B.max_dn = max_dn;
+  B.vec2 = (nd % 2 == 0) ? 1 : 0;
+  auto up = [&](auto** dst, const void* src, size_t bytes) -> ed_status {
+    ED_CUDA(cudaMalloc((void**)dst, std::max<size_t>(bytes, 8)));
+    if (bytes) ED_CUDA(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, s));
+    return ED_OK;
+  };
+  ED_TRY(up(&B.up_off, boff.data(), boff.size() * 4));
+  ED_TRY(up(&B.up_npos, bnpos.data(), bnpos.size() * 4));
+  ED_TRY(up(&B.up_idx, bidx.data(), bidx.size() * 4));
+  ED_TRY(up(&B.dn_tab, tab.data(), tab.size() * 2));
+  if (!diag64) {
+    ED_TRY(up(&B.e_up_int, eui.data(), eui.size() * 4));
+    ED_TRY(up(&B.e_dn_int, edi.data(), edi.size() * 4));
+  } else {
+    ED_TRY(up(&B.e_up_fx, euf.data(), euf.size() * 8));
+    ED_TRY(up(&B.e_dn_fx, edf.data(), edf.size() * 8));
+  }
+  ED_CUDA(cudaStreamSynchronize(s));
+  B.eligible = 1;
+  return ED_OK;
+}
+
+void free_bfp(ed_plan_s* p) {
+  BfpTables& B = p->bfp;
+  cudaFree(B.up_off); cudaFree(B.up_npos); cudaFree(B.up_idx); cudaFree(B.dn_tab);
+  cudaFree(B.e_up_int); cudaFree(B.e_dn_int); cudaFree(B.e_up_fx); cudaFree(B.e_dn_fx);
+  B = BfpTables();
+}
+
+static BfpHubArgs bfp_args(const ed_plan_s* p) {
+  const BfpTables& B = p->bfp;
+  BfpHubArgs a;
+  a.nu = p->num_up; a.nd = p->num_dn;
+  a.up_off = B.up_off; a.up_npos = B.up_npos; a.up_idx = B.up_idx;
+  a.dn_tab = B.dn_tab; a.max_dn = B.max_dn;
+  a.up_states = p->up.states; a.dn_states = p->dn.states;
+  a.e_up = B.e_up_int; a.e_dn = B.e_dn_int;
+  a.u_uniform = B.u_uniform; a.u0 = B.u0_int;
+  for (int i = 0; i < ED_MAX_SITES + 2; ++i) a.u[i] = B.u_int[i];
+  a.t_int = B.t_int; a.F = B.F;
+  a.e_up_fx = B.e_up_fx; a.e_dn_fx = B.e_dn_fx;
+  a.u0_fx = B.u0_fx;
+  for (int i = 0; i < ED_MAX_SITES + 2; ++i) a.u_fx[i] = B.u_fx[i];
+  a.dshift = B.Fd - B.F;
+  return a;
+}
+
+constexpr int MV_NT = 256;
+
+static int bfp_matvec_grid(const ed_plan_s* p) {
+  const size_t smem = (2 * p->num_dn + 1) * sizeof(int64_t);
+  int per_sm = (int)std::max<size_t>(1, (200 * 1024) / std::max<size_t>(smem, 1));
+  per_sm = std::min(per_sm, 2048 / MV_NT);
+  return (int)std::min<int64_t>(p->num_up, (int64_t)p->ctx->num_sms * per_sm);
+}
+
+// opt-in to large dynamic shared memory once per (kernel variant, device)
+template <bool VEC2, bool DIAG64>
+static ed_status launch_variant(const ed_plan_s* p, size_t smem, int g, const int64_t* X, int64_t* W,
+                                double* partial, unsigned long long* partial_max, BfpState* st, cudaStream_t s) {
+  static std::atomic<uint64_t> done{0};
+  const uint64_t bit = 1ull << (p->device & 63);
+  if (!(done.load() & bit)) {
+    ED_CUDA(cudaFuncSetAttribute(k_bfp_hub_matvec<MV_NT, VEC2, DIAG64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024));
+    done.fetch_or(bit);
+  }
+  k_bfp_hub_matvec<MV_NT, VEC2, DIAG64><<<g, MV_NT, smem, s>>>(bfp_args(p), X, W, partial, partial_max, st);
+  ED_CHECK_LAUNCH("k_bfp_hub_matvec");
+  return ED_OK;
+}
+
+static ed_status launch_bfp_matvec(const ed_plan_s* p, const int64_t* X, int64_t* W, double* partial,
+                                   unsigned long long* partial_max, BfpState* st, cudaStream_t s) {
+  const size_t smem = (2 * p->num_dn + 1) * sizeof(int64_t);
+  const int g = bfp_matvec_grid(p);
+  const bool v2 = p->bfp.vec2 != 0, d64 = p->bfp.diag64 != 0;
+  if (v2 && !d64) return launch_variant<true, false>(p, smem, g, X, W, partial, partial_max, st, s);
+  if (v2 && d64) return launch_variant<true, true>(p, smem, g, X, W, partial, partial_max, st, s);
+  if (!v2 && !d64) return launch_variant<false, false>(p, smem, g, X, W, partial, partial_max, st, s);
+  return launch_variant<false, true>(p, smem, g, X, W, partial, partial_max, st, s);
+}
+
+// ---- the BFP Lanczos driver ----------------------------------------------------------------------
+struct BfpLayout {
+  size_t off_R, off_W, off_eR, off_maxR, off_part, off_partmax, off_c, off_C, off_work, off_state, off_misc, total;
+  int nslots, nparts;
+};
+
+static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static BfpLayout bfp_layout(const ed_plan_s* p, int K, bool store) {
+  BfpLayout L;
+  const int64_t D = p->dim;
+  L.nslots = store ? K + 1 : 3;
+  L.nparts = std::max(bfp_matvec_grid(p), p->ctx->num_sms * 4);
+  size_t o = 0;
+  L.off_R = o; o = al256(o + (size_t)L.nslots * D * 8);
+  L.off_W = o; o = al256(o + (size_t)D * 8);
+  L.off_eR = o; o = al256(o + (size_t)(K + 2) * 4);
+  L.off_maxR = o; o = al256(o + (size_t)(K + 2) * 8);
+  L.off_part = o; o = al256(o + (size_t)L.nparts * 8);
+  L.off_partmax = o; o = al256(o + (size_t)L.nparts * 8);
+  L.off_c = o; o = al256(o + (size_t)(K + 2) * 8);
+  L.off_C = o; o = al256(o + (size_t)(K + 2) * 8);
+  L.off_work = o; o = al256(o + (size_t)5 * (K + 2) * 8);
+  L.off_state = o; o = al256(o + sizeof(BfpState));
+  L.off_misc = o; o = al256(o + 64);
+  L.total = o;
+  return L;
+}
+
+size_t bfp_workspace_bytes(const ed_plan_s* p, int K, bool store) { return bfp_layout(p, K, store).total; }
+
+// T_m of the fixed-point run: alpha[0..m), couplings beta[1..m) (beta[0] is the start norm,
+// which tridiag_lowest_block never reads).
+__global__ void k_lz_check_bfp(const double* alpha, const double* beta, int k, double tol, BfpState* st, double* c,
+                               double* work) {
+  if (*(volatile int*)&st->stop) return;
+  const double e = tridiag_lowest_block(alpha, beta, k + 1, c, work);
+  if (threadIdx.x == 0) {
+    const double res = fabs(beta[k + 1] * c[k]);
+    if (res <= tol * fmax(1.0, fabs(e))) { st->stop = 1; st->steps = k + 1; }
+    st->e_prev = e;
+    st->energy = e;
+    st->residual = res;
+  }
+}
+
+__global__ void k_lz_final_bfp(const double* alpha, const double* beta, int kmax, BfpState* st, double* c,
+                               double* work) {
+  const int m = st->stop ? st->steps : kmax;
+  const double e = tridiag_lowest_block(alpha, beta, m, c, work);
+  if (threadIdx.x == 0) {
+    st->energy = e;
+    st->steps = m;
+    st->residual = fabs(beta[m] * c[m - 1]);
+  }
+}
+
+struct BfpRun {
+  BfpLayout L;
+  BfpVecs v;
+  int64_t* W;
+  double *part, *c, *work;
+  unsigned long long* partmax;
+  int64_t* C;
+  BfpState* st;
+  int* misc;
+};
+
+static BfpRun bfp_bind(const ed_plan_s* p, void* work, int K, bool store) {
+  BfpRun r;
+  r.L = bfp_layout(p, K, store);
+  char* b = (char*)work;
+  r.v.R = (int64_t*)(b + r.L.off_R);
+  r.v.eR = (int32_t*)(b + r.L.off_eR);
+  r.v.maxR = (unsigned long long*)(b + r.L.off_maxR);
+  r.v.store = store ? 1 : 0;
+  r.v.D = p->dim;
+  r.W = (int64_t*)(b + r.L.off_W);
+  r.part = (double*)(b + r.L.off_part);
+  r.partmax = (unsigned long long*)(b + r.L.off_partmax);
+  r.c = (double*)(b + r.L.off_c);
+  r.C = (int64_t*)(b + r.L.off_C);
+  r.work = (double*)(b + r.L.off_work);
+  r.st = (BfpState*)(b + r.L.off_state);
+  r.misc = (int*)(b + r.L.off_misc);
+  return r;
+}
+
+// start vector (FP64, device) -> R_0 in BFP, beta_0 = ||v0||
+static ed_status bfp_start(const ed_plan_s* p, BfpRun& r, const double* v0, double* beta, cudaStream_t s) {
+  const int64_t D = p->dim;
+  const int gs = grid_for(D, 256, p->ctx->num_sms * 8);
+  unsigned long long* mxb = (unsigned long long*)(r.misc + 8);
+  ED_CUDA(cudaMemsetAsync(mxb, 0, 8, s));
+  k_maxabs_f64<<<gs, BT, 0, s>>>(v0, D, mxb);
+  k_f64_to_bfp<<<gs, 256, 0, s>>>(v0, D, mxb, p->bfp.m_in, r.v.vec(0), r.v.eR, r.v.maxR);
+  k_bfp_norm<<<r.L.nparts, BT, 0, s>>>(r.v, 0, r.part, r.st, beta);
+  ED_CHECK_LAUNCH_N("bfp start", 3);
+  unsigned long long hm = 0;
+  ED_CUDA(cudaMemcpyAsync(&hm, mxb, 8, cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  const double mx = *(double*)&hm;
+  if (!std::isfinite(mx)) return fail(ED_ERR_NONFINITE, "start vector is not finite");
+  if (mx == 0.0) return fail(ED_ERR_ZERO_VECTOR, "start vector has zero norm");
+  return ED_OK;
+}
+
+// one Lanczos step k: matvec + scalars + update (3 launches)
+static ed_status bfp_step(const ed_plan_s* p, BfpRun& r, int k, double* alpha, double* beta, cudaStream_t s) {
+  const int gmv = bfp_matvec_grid(p);
+  ED_TRY(launch_bfp_matvec(p, r.v.vec(k), r.W, r.part, r.partmax, r.st, s));
+  k_bfp_scalars<<<1, BT, 0, s>>>(r.v, k, p->bfp.F, p->bfp.m_in, r.part, r.partmax, gmv, alpha, beta, r.st);
+  k_bfp_update<<<r.L.nparts, BT, 0, s>>>(r.v, k, r.W, r.part, r.partmax, beta, alpha, r.st, 0);
+  ED_CHECK_LAUNCH_N("bfp step", 2);
+  return ED_OK;
+}
+
+}  // namespace ed
+
+using namespace ed;
+
+// Internal entry points used by ed_lanczos / ed_lanczos_coeffs (ed_lanczos.cu).
+namespace ed {
+
+ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const double* v0_dev, void* work,
+                      double* alpha, double* beta, double* evec, ed_lanczos_result* res, cudaStream_t s,
+                      double* v0_tmp /* FP64[D] scratch when v0 is generated */) {
+  const int K = prm->max_steps;
+  const int64_t D = p->dim;
+  const bool store = prm->want_vector != 0;
+  BfpRun r = bfp_bind(p, work, K, store);
+  ED_CUDA(cudaMemsetAsync(r.st, 0, sizeof(BfpState), s));
+  ED_CUDA(cudaMemsetAsync(alpha, 0, K * sizeof(double), s));
+  ED_CUDA(cudaMemsetAsync(beta, 0, (K + 1) * sizeof(double), s));
+  ED_TRY(bfp_start(p, r, v0_dev, beta, s));
+  const int Km = (int)std::min<int64_t>(K, D);
+  std::vector<cudaEvent_t> ev;
+  if (prm->profile) {
+    ev.resize(2 * (size_t)Km);
+    for (auto& e : ev) ED_CUDA(cudaEventCreate(&e));
+  }
+  for (int k = 0; k < Km; ++k) {
+    if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k], s));
+    ED_TRY(launch_bfp_matvec(p, r.v.vec(k), r.W, r.part, r.partmax, r.st, s));
+    if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k + 1], s));
+    k_bfp_scalars<<<1, BT, 0, s>>>(r.v, k, p->bfp.F, p->bfp.m_in, r.part, r.partmax, bfp_matvec_grid(p), alpha,
+                                   beta, r.st);
+    k_bfp_update<<<r.L.nparts, BT, 0, s>>>(r.v, k, r.W, r.part, r.partmax, beta, alpha, r.st, 0);
+    uint64_t nl = 2;
+    if (prm->check_every > 0 && ((k + 1) % prm->check_every == 0) && k + 1 < Km) {
+      k_lz_check_bfp<<<1, 256, 0, s>>>(alpha, beta, k, prm->tol, r.st, r.c, r.work);
+      ++nl;
+    }
+    ED_CHECK_LAUNCH_N("bfp lanczos step", nl);
+  }
+  k_lz_final_bfp<<<1, 256, 0, s>>>(alpha, beta, Km, r.st, r.c, r.work);
+  ED_CHECK_LAUNCH("k_lz_final_bfp");
+  if (evec) {
+    k_bfp_ritz_coeffs<<<1, 32, 0, s>>>(r.v, r.c, beta, r.st, r.C, r.misc);
+    k_bfp_ritz<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(r.v, r.C, r.misc, r.st, evec);
+    ED_CHECK_LAUNCH_N("bfp ritz", 2);
+  }
+  BfpState hs;
+  ED_CUDA(cudaMemcpyAsync(&hs, r.st, sizeof(BfpState), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  res->energy = hs.energy;
+  res->residual = hs.residual;
+  res->steps = hs.steps;
+  res->converged = hs.stop;
+  res->status = hs.status;
+  res->matvec_ms = 0.0;
+  res->matvecs = 0;
+  if (prm->profile) {
+    for (int k = 0; k < hs.steps; ++k) {
+      float ms = 0.f;
+      ED_CUDA(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));
+      res->matvec_ms += ms;
+      res->matvecs += 1;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+  }
+  (void)v0_tmp;
+  return ED_OK;
+}
+
+ed_status bfp_lanczos_coeffs(const ed_plan_s* p, int K, const double* start, void* work, double* alpha,
+                             double* beta, int* steps, double* norm, cudaStream_t s) {
+  const int64_t D = p->dim;
+  BfpRun r = bfp_bind(p, work, K, false);
+  ED_CUDA(cudaMemsetAsync(r.st, 0, sizeof(BfpState), s));
+  ED_CUDA(cudaMemsetAsync(alpha, 0, K * sizeof(double), s));
+  ED_CUDA(cudaMemsetAsync(beta, 0, (K + 1) * sizeof(double), s));
+  // a zero start vector has an empty Krylov space
+  {
+    const int gs = grid_for(D, 256, p->ctx->num_sms * 8);
+    unsigned long long* mxb = (unsigned long long*)(r.misc + 8);
+    ED_CUDA(cudaMemsetAsync(mxb, 0, 8, s));
+    k_maxabs_f64<<<gs, BT, 0, s>>>(start, D, mxb);
+    ED_CHECK_LAUNCH("k_maxabs_f64");
+    unsigned long long hm = 0;
+    ED_CUDA(cudaMemcpyAsync(&hm, mxb, 8, cudaMemcpyDeviceToHost, s));
+    ED_CUDA(cudaStreamSynchronize(s));
+    const double mx = *(double*)&hm;
+    if (!std::isfinite(mx)) return fail(ED_ERR_NONFINITE, "start vector is not finite");
+    if (mx == 0.0) { *steps = 0; *norm = 0.0; return ED_OK; }
+  }
+  ED_TRY(bfp_start(p, r, start, beta, s));
+  const int Km = (int)std::min<int64_t>(K, D);
+  for (int k = 0; k < Km; ++k) ED_TRY(bfp_step(p, r, k, alpha, beta, s));
+  BfpState hs;
+  double b0 = 0.0;
+  ED_CUDA(cudaMemcpyAsync(&hs, r.st, sizeof(BfpState), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(&b0, beta, sizeof(double), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  *steps = hs.stop ? hs.steps : Km;
+  *norm = b0;
+  // the continued fraction expects beta[0] = 0 and beta[k] the couplings
+  ED_CUDA(cudaMemsetAsync(beta, 0, sizeof(double), s));
+  return ED_OK;
+}
+
+}  // namespace ed
+
+extern "C" {
+
+ED_API ed_status ed_fixed_from_f64(const double* d_x, int64_t n, int m_bits, int64_t* d_xm, int32_t* h_exp,
+                                   ed_stream_t stream) {
+  if (n < 0 || m_bits < 1 || m_bits > 62) return fail(ED_ERR_INVALID_ARG, "bad n / m_bits");
+  if (n == 0) { *h_exp = 0; return ED_OK; }
+  if (!d_x || !d_xm || !h_exp) return fail(ED_ERR_INVALID_ARG, "null argument");
+  DeviceContext* ctx;
+  ED_TRY(device_context(&ctx));
+  cudaStream_t s = as_stream(stream);
+  unsigned long long* tmp = nullptr;
+  ED_CUDA(cudaMallocAsync(&tmp, 32, s));
+  ED_CUDA(cudaMemsetAsync(tmp, 0, 32, s));
+  const int g = grid_for(n, 256, ctx->num_sms * 8);
+  k_maxabs_f64<<<g, BT, 0, s>>>(d_x, n, tmp);
+  k_f64_to_bfp<<<g, 256, 0, s>>>(d_x, n, tmp, m_bits, d_xm, (int32_t*)(tmp + 1), tmp + 2);
+  ED_CHECK_LAUNCH_N("ed_fixed_from_f64", 2);
+  unsigned long long h[3];
+  ED_CUDA(cudaMemcpyAsync(h, tmp, 24, cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  ED_CUDA(cudaFreeAsync(tmp, s));
+  const double mx = *(double*)&h[0];
+  if (!std::isfinite(mx)) return fail(ED_ERR_NONFINITE, "input is not finite");
+  *h_exp = *(int32_t*)&h[1];
+  return ED_OK;
+}
+
+ED_API ed_status ed_fixed_to_f64(const int64_t* d_xm, int64_t n, int32_t exp, double* d_x, ed_stream_t stream) {
+  if (n < 0) return fail(ED_ERR_INVALID_ARG, "negative n");
+  if (n == 0) return ED_OK;
+  if (!d_xm || !d_x) return fail(ED_ERR_INVALID_ARG, "null argument");
+  DeviceContext* ctx;
+  ED_TRY(device_context(&ctx));
+  cudaStream_t s = as_stream(stream);
+  int32_t* e = nullptr;
+  ED_CUDA(cudaMallocAsync(&e, 4, s));
+  ED_CUDA(cudaMemcpyAsync(e, &exp, 4, cudaMemcpyHostToDevice, s));
+  k_bfp_to_f64<<<grid_for(n, 256, ctx->num_sms * 8), 256, 0, s>>>(d_xm, e, n, d_x);
+  ED_CHECK_LAUNCH("k_bfp_to_f64");
+  ED_CUDA(cudaFreeAsync(e, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  return ED_OK;
+}
+
+ED_API ed_status ed_matvec_fixed(ed_plan p, const int64_t* d_xm, int32_t ex, int64_t* d_wm, int32_t* h_ew,
+                                 int* h_m_in, ed_stream_t stream) {
+  ED_TRY(check_plan(p));
+  if (!p->bfp.eligible) return fail(ED_ERR_INVALID_ARG, "sector has no fixed-point matvec (needs one hopping magnitude and dyadic coefficients)");
+  if (h_m_in) *h_m_in = p->bfp.m_in;
+  if (h_ew) *h_ew = ex - p->bfp.F;
+  if (p->dim == 0) return ED_OK;
+  if (!d_xm || !d_wm) return fail(ED_ERR_INVALID_ARG, "null vector");
+  if (d_xm == d_wm) return fail(ED_ERR_INVALID_ARG, "x and w must not alias");
+  return launch_bfp_matvec(p, d_xm, d_wm, nullptr, nullptr, nullptr, as_stream(stream));
+}
+
+ED_API int ed_plan_fixed_point(ed_plan p) { return (p && p->bfp.eligible) ? p->bfp.m_in : 0; }
+
+}  // extern "C"

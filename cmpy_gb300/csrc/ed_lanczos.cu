@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "ed_plan.cuh"
+#include "ed_tridiag.cuh"
 
 namespace ed {
 
@@ -187,134 +188,6 @@ __global__ void k_multiaxpy(const double* __restrict__ Q, int64_t ldq, int m, co
   }
 }
 
-// ---- symmetric tridiagonal eigen-solver (one block) ----------------------------------------
-// Number of eigenvalues of T (alpha[0..m), beta[1..m)) below x: sign changes of the LDL^T
-// pivots, computed without divisions by rescaling a three-term recurrence.
-__device__ int sturm_count(const double* a, const double* b, int m, double x) {
-  // p_i = (a_i - x) p_{i-1} - b_i^2 p_{i-2}; count sign changes of p_i / p_{i-1}
-  // a zero p_i is replaced by a tiny value of the opposite sign of p_{i-1} (a tiny negative
-  // pivot), the usual convention for an eigenvalue exactly at x
-  double p0 = 1.0, p1 = a[0] - x;
-  if (p1 == 0.0) p1 = -0x1.0p-900;
-  int cnt = (p1 < 0.0) ? 1 : 0;
-  for (int i = 1; i < m; ++i) {
-    const double bb = b[i] * b[i];
-    double p2 = (a[i] - x) * p1 - bb * p0;
-    if (p2 == 0.0) p2 = -p1 * 0x1.0p-60;
-    if ((p2 < 0.0) != (p1 < 0.0)) ++cnt;
-    // rescale to avoid overflow/underflow (exact powers of two)
-    const double ap = fabs(p2);
-    if (ap > 0x1.0p+400 || ap < 0x1.0p-400) {
-      const int e = ilogb(ap);
-      p2 = scalbn(p2, -e);
-      p1 = scalbn(p1, -e);
-    }
-    p0 = p1;
-    p1 = p2;
-  }
-  return cnt;
-}
-
-// Lowest eigenvalue by 32-way multisection (warp 0 evaluates the Sturm counts; FP64 is a
-// scarce pipe on this GPU, so fewer points per round cost less in total), then optionally
-// the eigenvector by inverse iteration (thread 0, FP64, partial pivoting).
-constexpr int MS_PTS = 32;
-__device__ double tridiag_lowest_block(const double* a, const double* b, int m, double* vec, double* work) {
-  __shared__ double lo_s, hi_s;
-  __shared__ int cnt_s[MS_PTS];
-  if (threadIdx.x == 0) {
-    double lo = a[0], hi = a[0];
-    for (int i = 0; i < m; ++i) {
-      const double r = (i > 0 ? fabs(b[i]) : 0.0) + (i + 1 < m ? fabs(b[i + 1]) : 0.0);
-      lo = fmin(lo, a[i] - r);
-      hi = fmax(hi, a[i] + r);
-    }
-    const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
-    lo_s = lo - pad;
-    hi_s = hi + pad;
-  }
-  __syncthreads();
-  for (int round = 0; round < 16; ++round) {
-    const double lo = lo_s, hi = hi_s;
-    if (threadIdx.x < MS_PTS) {
-      const double x = lo + (hi - lo) * (double)(threadIdx.x + 1) / (double)(MS_PTS + 1);
-      cnt_s[threadIdx.x] = sturm_count(a, b, m, x);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int t = 0;
-      while (t < MS_PTS && cnt_s[t] == 0) ++t;  // first point with >=1 eigenvalue below
-      const double nlo = (t == 0) ? lo : lo + (hi - lo) * (double)t / (double)(MS_PTS + 1);
-      const double nhi = (t == MS_PTS) ? hi : lo + (hi - lo) * (double)(t + 1) / (double)(MS_PTS + 1);
-      lo_s = nlo;
-      hi_s = nhi;
-    }
-    __syncthreads();
-    if (hi_s - lo_s <= 4e-16 * fmax(fabs(lo_s), fabs(hi_s)) + 1e-300) break;
-  }
-  const double ev = 0.5 * (lo_s + hi_s);
-  if (vec && threadIdx.x == 0) {
-    // inverse iteration: (T - ev I) y = v, Gaussian elimination with partial pivoting.
-    // work: 5*m doubles (diag, super, super2, sub multipliers, pivot flags)
-    double* dd = work;           // diagonal of U
-    double* du = work + m;       // first super-diagonal of U
-    double* du2 = work + 2 * m;  // second super-diagonal of U
-    double* ml = work + 3 * m;   // multipliers
-    double* pv = work + 4 * m;   // 1.0 if rows swapped at step i
-    const double tiny = 1e-300 + 1e-15 * fmax(fabs(ev), 1.0) * 1e-3;
-    for (int i = 0; i < m; ++i) vec[i] = 1.0 / sqrt((double)m) * (1.0 + 0.01 * (double)((i * 7919) % 13) / 13.0);
-    for (int it = 0; it < 3; ++it) {
-      // factor T - ev I (rebuilt each iteration; m is small)
-      for (int i = 0; i < m; ++i) { dd[i] = a[i] - ev; du[i] = (i + 1 < m) ? b[i + 1] : 0.0; du2[i] = 0.0; }
-      for (int i = 0; i < m - 1; ++i) {
-        const double sub = b[i + 1];
-        if (fabs(dd[i]) >= fabs(sub)) {
-          pv[i] = 0.0;
-          if (dd[i] == 0.0) dd[i] = tiny;
-          const double l = sub / dd[i];
-          ml[i] = l;
-          dd[i + 1] -= l * du[i];
-        } else {
-          pv[i] = 1.0;
-          const double l = dd[i] / sub;
-          ml[i] = l;
-          // swap rows i and i+1
-          const double t0 = dd[i + 1], t1 = (i + 2 < m) ? du[i + 1] : 0.0;
-          dd[i] = sub;
-          const double odu = du[i];
-          du[i] = t0;
-          du2[i] = t1;
-          dd[i + 1] = odu - l * t0;
-          if (i + 2 < m) du[i + 1] = -l * t1;
-        }
-      }
-      if (dd[m - 1] == 0.0) dd[m - 1] = tiny;
-      // forward: apply L^-1 to vec
-      for (int i = 0; i < m - 1; ++i) {
-        if (pv[i] != 0.0) { const double t = vec[i]; vec[i] = vec[i + 1]; vec[i + 1] = t - ml[i] * vec[i]; }
-        else vec[i + 1] -= ml[i] * vec[i];
-      }
-      // back substitution
-      for (int i = m - 1; i >= 0; --i) {
-        double s = vec[i];
-        if (i + 1 < m) s -= du[i] * vec[i + 1];
-        if (i + 2 < m) s -= du2[i] * vec[i + 2];
-        vec[i] = s / dd[i];
-      }
-      double nrm = 0.0;
-      for (int i = 0; i < m; ++i) nrm = fma(vec[i], vec[i], nrm);
-      nrm = 1.0 / sqrt(nrm);
-      for (int i = 0; i < m; ++i) vec[i] *= nrm;
-    }
-    // sign convention: first nonzero component positive
-    double sg = 1.0;
-    for (int i = 0; i < m; ++i) if (vec[i] != 0.0) { sg = vec[i] > 0 ? 1.0 : -1.0; break; }
-    for (int i = 0; i < m; ++i) vec[i] *= sg;
-  }
-  __syncthreads();
-  return ev;
-}
-
 // convergence check after step k (T has size k+1): Ritz residual |beta_{k+1} * s_k| of the
 // lowest Ritz pair, relative to max(1, |E|)
 __global__ void k_lz_check(const double* alpha, const double* beta, int k, double tol, LzState* st, double* c,
@@ -393,12 +266,33 @@ using namespace ed;
 
 extern "C" {
 
+// fixed-point vectors: automatic when the sector allows them and no reorthogonalisation
+static ed_status use_fixed(const ed_plan_s* p, const ed_lanczos_params* prm, bool* out) {
+  const bool ok = p->bfp.eligible && !prm->reorth;
+  if (prm->arithmetic == 2 && !ok)
+    return fail(ED_ERR_INVALID_ARG, "fixed-point Lanczos needs a fixed-point sector and reorth = 0");
+  *out = ok && prm->arithmetic != 1;
+  return ED_OK;
+}
+
 ED_API ed_status ed_lanczos_workspace(ed_plan p, const ed_lanczos_params* prm, size_t* bytes) {
   ED_TRY(check_plan(p));
   if (!prm || !bytes) return fail(ED_ERR_INVALID_ARG, "null argument");
   if (prm->max_steps < 1 || prm->max_steps > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  bool fixed = false;
+  ED_TRY(use_fixed(p, prm, &fixed));
   const bool store = prm->want_vector || prm->reorth;
-  *bytes = lz_layout(p->dim, prm->max_steps, store, lz_parts(p, p->dim)).total;
+  *bytes = fixed ? bfp_workspace_bytes(p, prm->max_steps, store)
+                 : lz_layout(p->dim, prm->max_steps, store, lz_parts(p, p->dim)).total;
+  return ED_OK;
+}
+
+// normalises d_evec in place (FP64)
+static ed_status normalise(const ed_plan_s* p, double* v, int64_t D, double* part, double* scal, LzState* st,
+                           cudaStream_t s) {
+  k_dot<<<lz_parts(p, D), LZ_NT, 0, s>>>(v, v, D, part, st, 0, scal, scal + 1, nullptr);
+  k_scale<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(v, v, D, scal + 1, nullptr);
+  ED_CHECK_LAUNCH_N("normalise", 2);
   return ED_OK;
 }
 
@@ -412,6 +306,41 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
   const int64_t D = p->dim;
   if (D < 1) return fail(ED_ERR_INVALID_ARG, "empty sector");
   if (prm->want_vector && !d_evec) return fail(ED_ERR_INVALID_ARG, "want_vector needs d_evec");
+  bool fixed = false;
+  ED_TRY(use_fixed(p, prm, &fixed));
+  if (fixed) {
+    const size_t need = bfp_workspace_bytes(p, K, prm->want_vector != 0);
+    if (!d_work || work_bytes < need) return fail(ED_ERR_INVALID_ARG, "workspace too small (see ed_lanczos_workspace)");
+    cudaStream_t s = as_stream(stream);
+    // FP64 start vector: the caller's, else a seeded uniform(0,1) one generated into d_evec
+    // (overwritten by the Ritz vector at the end) or into a temporary buffer
+    const double* v0 = d_v0;
+    double* tmp_alloc = nullptr;
+    if (!v0) {
+      double* tmp = d_evec;
+      if (!tmp) {
+        ED_CUDA(cudaMallocAsync(&tmp_alloc, D * sizeof(double), s));
+        tmp = tmp_alloc;
+      }
+      k_random_start<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(tmp, D, prm->seed);
+      ED_CHECK_LAUNCH("k_random_start");
+      v0 = tmp;
+    }
+    const ed_status rs = bfp_lanczos(p, prm, v0, d_work, d_alpha, d_beta, d_evec, res, s, nullptr);
+    if (tmp_alloc) cudaFreeAsync(tmp_alloc, s);
+    ED_TRY(rs);
+    if (d_evec) {
+      double* scratch = nullptr;
+      ED_CUDA(cudaMallocAsync(&scratch, (lz_parts(p, D) + 8) * sizeof(double) + sizeof(LzState) + 256, s));
+      LzState* st = (LzState*)((char*)scratch + ((lz_parts(p, D) + 8) * sizeof(double) + 255) / 256 * 256);
+      ED_CUDA(cudaMemsetAsync(st, 0, sizeof(LzState), s));
+      ed_status r = normalise(p, d_evec, D, scratch, scratch + lz_parts(p, D), st, s);
+      ED_CUDA(cudaStreamSynchronize(s));
+      cudaFreeAsync(scratch, s);
+      ED_TRY(r);
+    }
+    return ED_OK;
+  }
   const bool store = prm->want_vector || prm->reorth;
   const int nparts = lz_parts(p, D);
   const LzLayout L = lz_layout(D, K, store, nparts);
@@ -528,6 +457,11 @@ ED_API ed_status ed_lanczos_coeffs(ed_plan p, int K, const double* d_start, void
   if (K < 1 || K > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
   const int64_t D = p->dim;
   if (D < 1) return fail(ED_ERR_INVALID_ARG, "empty sector");
+  if (p->bfp.eligible) {
+    if (!d_work || work_bytes < bfp_workspace_bytes(p, K, false))
+      return fail(ED_ERR_INVALID_ARG, "workspace too small (see ed_lanczos_workspace)");
+    return bfp_lanczos_coeffs(p, K, d_start, d_work, d_alpha, d_beta, h_steps, h_norm, as_stream(stream));
+  }
   const int nparts = lz_parts(p, D);
   const LzLayout L = lz_layout(D, K, false, nparts);
   if (!d_work || work_bytes < L.total) return fail(ED_ERR_INVALID_ARG, "workspace too small (see ed_lanczos_workspace)");

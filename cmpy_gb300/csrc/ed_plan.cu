@@ -41,7 +41,7 @@ __global__ void k_hop_count(const uint64_t* __restrict__ states, int64_t n, Bond
 
 __global__ void k_hop_fill(const uint64_t* __restrict__ tab, const uint64_t* __restrict__ states, int64_t n,
                            BondList bl, const int32_t* __restrict__ off, int32_t* __restrict__ idx,
-                           double* __restrict__ coef) {
+                           double* __restrict__ coef, int16_t* __restrict__ bond) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const uint64_t s = states[i];
     int64_t o = off[i];
@@ -51,6 +51,7 @@ __global__ void k_hop_fill(const uint64_t* __restrict__ tab, const uint64_t* __r
         idx[o] = (int32_t)colex_rank(tab, t);
         const int sg = hop_sign(s, bl.width, bl.s1[b], bl.s2[b]);
         coef[o] = sg < 0 ? -bl.hop[b] : bl.hop[b];
+        bond[o] = (int16_t)b;
         ++o;
       }
     }
@@ -130,7 +131,7 @@ __global__ void k_row_abs_max(const int32_t* __restrict__ off, const double* __r
 }
 
 static void free_table(SpinTable& t) {
-  cudaFree(t.states); cudaFree(t.energy); cudaFree(t.off); cudaFree(t.idx); cudaFree(t.coef);
+  cudaFree(t.states); cudaFree(t.energy); cudaFree(t.off); cudaFree(t.idx); cudaFree(t.coef); cudaFree(t.bond);
   t = SpinTable();
 }
 
@@ -173,7 +174,8 @@ static ed_status build_fermion_table(ed_plan_s* p, SpinTable& t, int n, cudaStre
   ED_CUDA(cudaMemcpyAsync(t.off, off.data(), (t.n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s));
   ED_CUDA(cudaMalloc(&t.idx, std::max<int64_t>(acc, 1) * sizeof(int32_t)));
   ED_CUDA(cudaMalloc(&t.coef, std::max<int64_t>(acc, 1) * sizeof(double)));
-  k_hop_fill<<<g, 256, 0, s>>>(p->ctx->d_binom, t.states, t.n, bl, t.off, t.idx, t.coef);
+  ED_CUDA(cudaMalloc(&t.bond, std::max<int64_t>(acc, 1) * sizeof(int16_t)));
+  k_hop_fill<<<g, 256, 0, s>>>(p->ctx->d_binom, t.states, t.n, bl, t.off, t.idx, t.coef, t.bond);
   ED_CHECK_LAUNCH("k_hop_fill");
   ED_CUDA(cudaStreamSynchronize(s));  // host `off` must outlive the copy
   return ED_OK;
@@ -416,6 +418,7 @@ ED_API ed_status ed_plan_create_fermion(const ed_fermion_model* m, int n_up, int
   st = build_fermion_table(p, p->up, n_up, s);
   if (st == ED_OK) st = build_fermion_table(p, p->dn, n_dn, s);
   if (st == ED_OK) st = finish_bounds(p, s);
+  if (st == ED_OK) st = build_bfp(p, s);
   if (st != ED_OK) { ed_plan_destroy(p); return st; }
   *out = p;
   return ED_OK;
@@ -492,6 +495,7 @@ ED_API ed_status ed_plan_destroy(ed_plan p) {
   if (p->device >= 0 && prev != p->device) cudaSetDevice(p->device);
   free_table(p->up);
   free_table(p->dn);
+  free_bfp(p);
   cudaFree(p->spin_diag);
   if (prev >= 0 && prev != p->device) cudaSetDevice(prev);
   delete p;

@@ -22,6 +22,7 @@ struct SpinTable {
   int32_t* off = nullptr;     // [n+1]
   int32_t* idx = nullptr;     // [nnz] target state index j
   double* coef = nullptr;     // [nnz] hop value with sign
+  int16_t* bond = nullptr;    // [nnz] bond of the entry (fermion tables)
   int32_t max_row = 0;        // longest row
 };
 
@@ -30,6 +31,39 @@ struct FermionParams {
   int u_uniform;   // 1 if all u[i] equal (then U-term = u0 * popcount)
   double u0;
   double u[ED_MAX_SITES + 2];
+};
+
+// Tables of the block-fixed-point (BFP) matvec. Eligible sectors have one hopping magnitude
+// |t| = t_int * 2^-F (t_int a small integer). Output exponent e_w = e_x - F and
+//   W = t_int * sum(+-X_nbr) + D(X)
+// for input mantissas |X| <= 2^m_in, where the diagonal term D is
+//   diag64 = 0: diag_int * X, exact (eps, U exact integers times 2^-F);
+//   diag64 = 1: round(diag_fx * X / 2^(Fd - F)) with diag_fx = diag * 2^Fd in int64
+//               (arbitrary FP64 on-site energies; one rounding per element).
+struct BfpTables {
+  int eligible = 0;
+  int F = 0;              // hopping scale: |t| = t_int * 2^-F
+  int m_in = 56;          // input mantissa bound 2^m_in
+  int32_t t_int = 0;      // hop magnitude as integer
+  int diag64 = 0;         // diagonal mode (see above)
+  int Fd = 0;             // diag64: fractional bits of diag_fx
+  int u_uniform = 1;
+  int32_t u0_int = 0;
+  int32_t u_int[ED_MAX_SITES + 2] = {};
+  int64_t u0_fx = 0;
+  int64_t u_fx[ED_MAX_SITES + 2] = {};
+  int64_t* e_up_fx = nullptr;  // diag64: [nu]
+  int64_t* e_dn_fx = nullptr;  // diag64: [nd]
+  int max_dn = 0;         // dn table entries per column (padded)
+  int vec2 = 0;           // num_dn even: 128-bit row loads
+  // up: per target row, neighbours with + sign first, then - sign
+  int32_t* up_off = nullptr;   // [nu+1]
+  int32_t* up_npos = nullptr;  // [nu]
+  int32_t* up_idx = nullptr;   // [nnz]
+  // dn: column-major [max_dn][nd] shared-memory slots: j (+), nd + j (-), 2*nd (zero)
+  uint16_t* dn_tab = nullptr;
+  int32_t* e_up_int = nullptr;  // [nu]
+  int32_t* e_dn_int = nullptr;  // [nd]
 };
 
 }  // namespace ed
@@ -54,6 +88,7 @@ struct ed_plan_s {
   ed::FermionParams fp;
   double* spin_diag = nullptr;  // spin: [D]
   ed::DeviceContext* ctx = nullptr;
+  ed::BfpTables bfp;
 };
 
 namespace ed {
@@ -62,4 +97,14 @@ ed_status check_plan(const ed_plan_s* p);
 // y = H x for nvec vectors (leading dimension ld); skipped when *stop != 0 (stop may be null).
 ed_status matvec_f64(const ed_plan_s* p, const double* x, double* y, int64_t nvec, int64_t ld, cudaStream_t s,
                      const int* stop = nullptr);
+// Builds p->bfp when the sector qualifies (called at plan creation; synchronous).
+ed_status build_bfp(ed_plan_s* p, cudaStream_t s);
+void free_bfp(ed_plan_s* p);
+// fixed-point Lanczos (ed_bfp.cu)
+size_t bfp_workspace_bytes(const ed_plan_s* p, int K, bool store);
+ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const double* v0_dev, void* work,
+                      double* alpha, double* beta, double* evec, ed_lanczos_result* res, cudaStream_t s,
+                      double* v0_tmp);
+ed_status bfp_lanczos_coeffs(const ed_plan_s* p, int K, const double* start, void* work, double* alpha,
+                             double* beta, int* steps, double* norm, cudaStream_t s);
 }  // namespace ed

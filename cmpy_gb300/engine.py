@@ -219,6 +219,20 @@ class Plan:
             N.check(N.lib().ed_matmat(self._h, N.ptr(Xc), N.ptr(Y), Xc.shape[0], self.dim, _stream()))
             return Y.t()
 
+    @property
+    def fixed_point(self) -> int:
+        """Input mantissa bits of the sector's integer matvec, 0 if it has none."""
+        return int(N.lib().ed_plan_fixed_point(self._h))
+
+    def matvec_fixed(self, xm: torch.Tensor, ex: int) -> tuple[torch.Tensor, int]:
+        """Exact integer H*x for x = xm * 2^ex (int64 mantissas); returns (wm, ew)."""
+        with self._dev():
+            xm = xm.to(device=device(), dtype=torch.int64).contiguous().reshape(-1)
+            wm = torch.empty_like(xm)
+            ew = C.c_int32()
+            N.check(N.lib().ed_matvec_fixed(self._h, N.ptr(xm), int(ex), N.ptr(wm), C.byref(ew), None, _stream()))
+            return wm, int(ew.value)
+
     def dense(self) -> torch.Tensor:
         with self._dev():
             out = torch.empty((self.dim, self.dim), dtype=torch.float64, device=device())
@@ -311,6 +325,22 @@ def coo_hopping(up_states, dn_states, width, site1, site2, hop):
                      int(site1), int(site2), float(hop))
 
 
+def fixed_from_f64(x, m_bits: int = 56) -> tuple[torch.Tensor, int]:
+    """Block-fixed-point encoding of an FP64 vector: (int64 mantissas, exponent)."""
+    xt = _as_dev_f64(x).reshape(-1)
+    xm = torch.empty(xt.numel(), dtype=torch.int64, device=xt.device)
+    e = C.c_int32()
+    N.check(N.lib().ed_fixed_from_f64(N.ptr(xt), xt.numel(), int(m_bits), N.ptr(xm), C.byref(e), _stream()))
+    return xm, int(e.value)
+
+
+def fixed_to_f64(xm: torch.Tensor, exp: int) -> torch.Tensor:
+    xm = xm.to(device=device(), dtype=torch.int64).contiguous()
+    out = torch.empty(xm.numel(), dtype=torch.float64, device=xm.device)
+    N.check(N.lib().ed_fixed_to_f64(N.ptr(xm), xm.numel(), int(exp), N.ptr(out), _stream()))
+    return out
+
+
 def csr_matvec(rowptr: torch.Tensor, cols: torch.Tensor, vals: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
     n = rowptr.numel() - 1
     y = torch.empty(n, dtype=torch.float64, device=x.device)
@@ -338,8 +368,12 @@ class LanczosResult:
 
 def lanczos(plan: Plan, max_steps: int = 250, reorth: bool = False, want_vector: bool = True,
             tol: float = 0.0, check_every: int = 0, v0: torch.Tensor | None = None, seed: int = 0,
-            workspace: torch.Tensor | None = None, profile: bool = False) -> LanczosResult:
-    """Lanczos ground state of a plan, entirely on the device."""
+            workspace: torch.Tensor | None = None, profile: bool = False,
+            arithmetic: str = "auto") -> LanczosResult:
+    """Lanczos ground state of a plan, entirely on the device.
+
+    arithmetic: "auto" (block-fixed-point vectors when the sector allows it), "f64" or
+    "fixed" (error if the sector has no integer matvec)."""
     L = N.lib()
     prm = N.LanczosParams()
     prm.max_steps = int(max_steps)
@@ -349,6 +383,7 @@ def lanczos(plan: Plan, max_steps: int = 250, reorth: bool = False, want_vector:
     prm.tol = float(tol)
     prm.seed = int(seed)
     prm.profile = int(bool(profile))
+    prm.arithmetic = {"auto": 0, "f64": 1, "fixed": 2}[arithmetic]
     with plan._dev():
         nb = C.c_size_t()
         N.check(L.ed_lanczos_workspace(plan.handle, C.byref(prm), C.byref(nb)))
@@ -388,10 +423,11 @@ def lanczos_coeffs(plan: Plan, start: torch.Tensor, max_steps: int = 200,
         return alpha[:m], beta[: m + 1], float(nrm.value)
 
 
-def tridiag_lowest(alpha: torch.Tensor, beta: torch.Tensor, want_vector: bool = True):
-    m = alpha.numel()
-    a = _as_dev_f64(alpha)
-    b = _as_dev_f64(beta)
+def tridiag_lowest(alpha, beta, want_vector: bool = True):
+    """Lowest eigenpair of the tridiagonal (alpha[0..m), beta[1..m)) on the device."""
+    a = _as_dev_f64(alpha).reshape(-1)
+    b = _as_dev_f64(beta).reshape(-1)
+    m = a.numel()
     if b.numel() < m:
         raise ValueError("beta needs at least len(alpha) entries (beta[0] unused)")
     val = torch.empty(1, dtype=torch.float64, device=device())

@@ -120,6 +120,18 @@ class LinearOperator(sla.LinearOperator, abc.ABC):
     def toarray(self) -> np.ndarray:
         return self.matmat(np.eye(self.shape[1], dtype=self.dtype))
 
+    # torch tensors (on the GPU) pass straight to the device implementation; everything
+    # else goes through scipy's checks like in the reference
+    def matvec(self, x):
+        if isinstance(x, torch.Tensor):
+            return self._matvec(x)
+        return super().matvec(x)
+
+    def matmat(self, X):
+        if isinstance(X, torch.Tensor):
+            return self._matmat(X)
+        return super().matmat(X)
+
     def _trace(self) -> float:
         return float(np.trace(self.toarray()))
 

@@ -224,7 +224,9 @@ typedef struct ed_lanczos_params {
   double tol;            /* stop when the Ritz residual |beta_m s_m| <= tol * max(1, |E|) */
   uint64_t seed;         /* start vector seed when d_v0 == NULL */
   int32_t profile;       /* 1 = time every matvec launch with CUDA events on `stream` */
-  int32_t reserved;
+  int32_t arithmetic;    /* 0 auto: block-fixed-point vectors when the sector allows it
+                            (ed_plan_fixed_point > 0, no reorth), else FP64;
+                            1 FP64 vectors; 2 fixed-point (error if the sector does not allow it) */
 } ed_lanczos_params;
 
 typedef struct ed_lanczos_result {
@@ -252,7 +254,9 @@ ED_API ed_status ed_lanczos(ed_plan plan, const ed_lanczos_params* params,
 
 /* Lanczos coefficients of the Krylov space of d_start (not normalised; its norm is
  * returned in *h_norm): the continued-fraction input of the Green's function. No basis is
- * stored (three vectors of workspace). Returns the number of steps in *h_steps. */
+ * stored (three vectors of workspace; size from ed_lanczos_workspace with want_vector = 0,
+ * reorth = 0, arithmetic = 0). Uses the fixed-point vectors when the sector allows it.
+ * Returns the number of steps in *h_steps. */
 ED_API ed_status ed_lanczos_coeffs(ed_plan plan, int max_steps, const double* d_start,
                                    void* d_work, size_t work_bytes, double* d_alpha,
                                    double* d_beta, int* h_steps, double* h_norm,
@@ -263,6 +267,62 @@ ED_API ed_status ed_lanczos_coeffs(ed_plan plan, int max_steps, const double* d_
  * d_vec (FP64[m]) may be NULL. */
 ED_API ed_status ed_tridiag_lowest(const double* d_alpha, const double* d_beta, int m,
                                    double* d_value, double* d_vec, ed_stream_t stream);
+
+/* ---- batched form: many sectors / realisations in one persistent launch -----------------
+ * No reference counterpart: the reference solves sectors one after another on the host
+ * (cmpy/exactdiag.py:24-43). A batch holds n fixed-point sector plans (ed_plan_fixed_point
+ * > 0; the plans must outlive the batch). One launch runs every problem's Lanczos in its own
+ * CTA (largest first from a device work queue); nothing in it allocates or synchronises with
+ * the host, so sequences of batched launches can be captured in a CUDA graph. */
+typedef struct ed_batch_s* ed_batch;
+ED_API ed_status ed_batch_create(const ed_plan* plans, int n, ed_batch* out);
+ED_API ed_status ed_batch_destroy(ed_batch batch);
+/* Workspace bytes for max_steps and a launch configuration (threads per CTA in
+ * {128,256,512,1024}, CTAs per SM); threads <= 0 uses the tuned (or default) configuration. */
+ED_API ed_status ed_batch_workspace(ed_batch batch, int max_steps, int threads, int ctas_per_sm,
+                                    size_t* h_bytes);
+/* Ground states of every problem. Outputs (device, problem p): alpha[p*K + k], beta[p*(K+1) + k]
+ * (beta[p*(K+1)] = start-vector norm), energy[p], residual[p], steps[p]. d_starts: optional
+ * DEVICE array of n device pointers to FP64 start vectors (NULL: seeded uniform(0,1)). With
+ * want_vector the normalised ground state of problem p is written to d_vecs + d_vec_offsets[p]
+ * (d_vec_offsets is a device array). tol/check_every as in ed_lanczos_params. Asynchronous. */
+ED_API ed_status ed_batch_lanczos(ed_batch batch, int max_steps, double tol, int check_every,
+                                  uint64_t seed, const double* const* d_starts, int want_vector,
+                                  void* d_work, size_t work_bytes, double* d_alpha, double* d_beta,
+                                  double* d_energy, double* d_residual, int32_t* d_steps,
+                                  double* d_vecs, const int64_t* d_vec_offsets, int threads,
+                                  int ctas_per_sm, ed_stream_t stream);
+/* Autotuner: times the candidate launch configurations on a tune_steps run and keeps the
+ * fastest for this batch (used when ed_batch_lanczos gets threads <= 0). Synchronous. */
+ED_API ed_status ed_batch_tune(ed_batch batch, int tune_steps, void* d_work, size_t work_bytes,
+                               double* d_alpha, double* d_beta, double* d_energy,
+                               double* d_residual, int32_t* d_steps, int* h_threads,
+                               int* h_ctas_per_sm, float* h_ms, ed_stream_t stream);
+/* Adds the continued fraction of every problem (layout of ed_batch_lanczos, norm^2 =
+ * beta[p*(K+1)]^2, shift d_e0[p]) at n_z frequencies into d_g[p*n_z + j] (complex FP64). */
+ED_API ed_status ed_batch_gf_continued_fraction(int n, int max_steps, const double* d_alpha,
+                                                const double* d_beta, const int32_t* d_steps,
+                                                const double* d_e0, int sign, const double* d_z,
+                                                int64_t n_z, double* d_g, ed_stream_t stream);
+
+/* ---- block-fixed-point vectors (no reference counterpart: GB300 arithmetic) ------------
+ * A vector is stored as int64 mantissas m[i] with one exponent e: x[i] = m[i] * 2^e. On
+ * GB300 the FP64 pipe is ~60x narrower than the integer pipe, so the engine's fast matvec
+ * and Lanczos run on these integer vectors (exact adds, 128-bit dot products).
+ *
+ * ed_plan_fixed_point: m_in > 0 (the input mantissa bound 2^m_in) when the sector has a
+ * fixed-point matvec (one hopping magnitude, eps/U/t exact integers times 2^-F), else 0. */
+ED_API int ed_plan_fixed_point(ed_plan plan);
+/* d_xm = round(d_x * 2^-e) with max |d_xm| < 2^m_bits; *h_exp = e. Synchronous. */
+ED_API ed_status ed_fixed_from_f64(const double* d_x, int64_t n, int m_bits, int64_t* d_xm,
+                                   int32_t* h_exp, ed_stream_t stream);
+/* d_x = d_xm * 2^exp. Synchronous. */
+ED_API ed_status ed_fixed_to_f64(const int64_t* d_xm, int64_t n, int32_t exp, double* d_x,
+                                 ed_stream_t stream);
+/* W = H X exactly in integers: input mantissas |d_xm| <= 2^m_in (m_in from
+ * ed_plan_fixed_point, also returned in *h_m_in), output exponent *h_ew = ex - F. */
+ED_API ed_status ed_matvec_fixed(ed_plan plan, const int64_t* d_xm, int32_t ex, int64_t* d_wm,
+                                 int32_t* h_ew, int* h_m_in, ed_stream_t stream);
 
 /* ---- Green's functions -------------------------------------------------------------- */
 
