@@ -152,6 +152,8 @@ _SIGNATURES = {
         [C.c_void_p, I32, P, C.c_size_t, P, P, P, P, P, C.POINTER(I32), C.POINTER(I32), C.POINTER(C.c_float), P],
     ),
     "ed_batch_gf_continued_fraction": (I32, [I32, I32, P, P, P, P, I32, P, I64, P, P]),
+    "ed_plan_num_params": (I32, [PLAN]),
+    "ed_param_sandwich": (I32, [PLAN, P, P, P, I32, P]),
     "ed_plan_fixed_point": (I32, [PLAN]),
     "ed_fixed_from_f64": (I32, [P, I64, I32, P, C.POINTER(C.c_int32), P]),
     "ed_fixed_to_f64": (I32, [P, I64, C.c_int32, P, P]),

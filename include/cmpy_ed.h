@@ -305,6 +305,17 @@ ED_API ed_status ed_batch_gf_continued_fraction(int n, int max_steps, const doub
                                                 const double* d_e0, int sign, const double* d_z,
                                                 int64_t n_z, double* d_g, ed_stream_t stream);
 
+/* ---- parameter derivatives (adjoint form; no reference counterpart) ---------------------
+ * Number of model parameters of a fermionic plan: 2*n_sites + n_bonds, in the order
+ * [eps_0..eps_{N-1}, U_0..U_{N-1}, t_0..t_{nb-1}] (cmpy/models/hubbard.py:13-22 and
+ * cmpy/models/anderson.py:147-158 give their meaning). */
+ED_API int ed_plan_num_params(ed_plan plan);
+/* d_out[theta] (+)= a^T (dH/dtheta) b for every parameter at once (a, b: FP64[D]);
+ * dH/deps_j = n_j_up + n_j_dn, dH/dU_j = n_j_up n_j_dn, dH/dt_b = the hopping of bond b with
+ * its fermionic sign. Supports n_sites <= 16, n_bonds <= 32. */
+ED_API ed_status ed_param_sandwich(ed_plan plan, const double* d_a, const double* d_b, double* d_out,
+                                   int accumulate, ed_stream_t stream);
+
 /* ---- block-fixed-point vectors (no reference counterpart: GB300 arithmetic) ------------
  * A vector is stored as int64 mantissas m[i] with one exponent e: x[i] = m[i] * 2^e. On
  * GB300 the FP64 pipe is ~60x narrower than the integer pipe, so the engine's fast matvec

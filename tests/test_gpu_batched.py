@@ -1,0 +1,131 @@
+"""GPU parity of the batched form: all sectors / many disorder realisations in one launch.
+
+Energies agree with the per-sector solver and the dense oracle to 1e-10 relative, ground-state
+vectors satisfy H psi = E psi, batched Green's functions match the per-problem continued
+fraction and the dense Lehmann oracle to 1e-8, graph replay is bitwise reproducible."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import ed_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _hub(N, periodic, **kw):
+    from cmpy_gb300.models import ChainLattice, HubbardModel
+
+    return HubbardModel(ChainLattice(N, periodic), **kw)
+
+
+def _dense(m, nu, nd):
+    eps, u, bonds, width = m.fermion_descriptor()
+    up, dn = O.sector_states(m.num_sites, nu), O.sector_states(m.num_sites, nd)
+    r, c, v = O.coo_fermion(up, dn, eps, u, bonds, width)
+    return O.dense_from_coo(len(up) * len(dn), r, c, v)
+
+
+def test_all_sectors_chain6(cuda, golden):
+    from cmpy_gb300.batched import groundstate_all_sectors
+
+    m = _hub(6, False, inter=4.0, mu=2.0)
+    fillings, res, b = groundstate_all_sectors(m, max_steps=300)
+    e = res.energy.cpu().numpy()
+    for (nu, nd), ei in zip(fillings, e):
+        ref = np.linalg.eigvalsh(_dense(m, nu, nd))[0]
+        assert abs(ei - ref) <= 1e-10 * max(1.0, abs(ref)), (nu, nd, ei, ref)
+    g = golden["exactdiag"]
+    i = int(np.argmin(e))
+    assert tuple(fillings[i]) == tuple(g["chain6_U4_sector"])
+    assert abs(e[i] - g["chain6_U4_E0"]) <= 1e-10 * abs(g["chain6_U4_E0"])
+    assert b.threads in (128, 256, 512, 1024)
+
+
+def test_all_sectors_ring10(cuda):
+    """The 121-sector sweep of the 10-site ring (U=6) against per-sector plain solves."""
+    from cmpy_gb300 import engine as E
+    from cmpy_gb300.batched import groundstate_all_sectors
+
+    m = _hub(10, True, inter=6.0, mu=3.0)
+    fillings, res, _ = groundstate_all_sectors(m, max_steps=300)
+    e = res.energy.cpu().numpy()
+    assert len(fillings) == 121
+    i = int(np.argmin(e))
+    assert tuple(fillings[i]) == (5, 5)
+    assert abs(e[i] - (-34.254559411302544)) <= 1e-10 * 34.25
+    for k in (0, 7, 33, 60, 88, 120):
+        nu, nd = fillings[k]
+        p = m.plan(nu, nd)
+        ref = E.lanczos(p, max_steps=min(300, p.dim), want_vector=False, tol=1e-12, check_every=10).energy
+        assert abs(e[k] - ref) <= 1e-10 * max(1.0, abs(ref)), (nu, nd)
+
+
+def test_batched_vectors_and_configs(cuda):
+    from cmpy_gb300.batched import Batch
+
+    rng = np.random.default_rng(2)
+    models = [_hub(8, False, inter=4.0, eps=rng.uniform(-1, 1, 8), mu=2.0) for _ in range(12)]
+    sectors = [tuple(rng.integers(2, 6, 2)) for _ in models]
+    plans = [m.plan(int(a), int(b)) for m, (a, b) in zip(models, sectors)]
+    b = Batch(plans)
+    r1 = b.lanczos(max_steps=300, want_vector=True)
+    for m, (nu, nd), p, ei, v in zip(models, sectors, plans, r1.energy.cpu().numpy(), r1.vectors):
+        ref = np.linalg.eigvalsh(_dense(m, int(nu), int(nd)))[0]
+        assert abs(ei - ref) <= 1e-10 * abs(ref)
+        assert abs(torch.linalg.norm(v).item() - 1) < 1e-12
+        assert torch.linalg.norm(p.matvec(v) - ei * v).item() < 1e-8 * abs(ei)
+    # every launch configuration gives the same energies
+    for th, ps in ((128, 4), (256, 2), (1024, 1)):
+        b.threads, b.ctas_per_sm = th, ps
+        r2 = b.lanczos(max_steps=300)
+        np.testing.assert_allclose(r2.energy.cpu().numpy(), r1.energy.cpu().numpy(), rtol=1e-12)
+
+
+def test_batched_gf_vs_dense(cuda):
+    from cmpy_gb300.batched import greens_functions_batched
+    from cmpy_gb300.exactdiag import gf_continued_fraction, groundstate_sector
+
+    rng = np.random.default_rng(4)
+    models = [_hub(6, False, inter=4.0, eps=rng.uniform(-1, 1, 6), mu=2.0) for _ in range(6)]
+    sectors = [(3, 3), (2, 3), (3, 2), (2, 2), (3, 4), (4, 3)]
+    z = np.concatenate([np.linspace(-8, 8, 128) + 0.05j, 1j * (2 * np.arange(64) + 1) * np.pi / 50.0])
+    e, g = greens_functions_batched(models, sectors, z, gf_levels=300)
+    g = g.cpu().numpy()
+    for i, (m, (nu, nd)) in enumerate(zip(models, sectors)):
+        e0, psi = groundstate_sector(m, nu, nd, max_steps=400, tol=1e-13)
+        assert abs(e[i].item() - e0) <= 1e-10 * abs(e0)
+        ref = gf_continued_fraction(m, z, nu, nd, e0, psi, pos=0, n_lev=300)
+        assert np.max(np.abs(g[i] - ref)) < 1e-8
+        # dense oracle
+        psi_h = psi.cpu().numpy()
+        up, dn = O.sector_states(6, nu), O.sector_states(6, nd)
+        cd = O.apply_fermion(up, dn, O.sector_states(6, nu + 1), dn, 0, 1, True, psi_h)
+        cm = O.apply_fermion(up, dn, O.sector_states(6, nu - 1), dn, 0, 1, False, psi_h)
+        dref = O.gf_zero_temperature_dense(None, _dense(m, nu + 1, nd), _dense(m, nu - 1, nd), cd, cm, e0, z)
+        assert np.max(np.abs(g[i] - dref)) < 1e-8
+
+
+def test_batch_graph_replay(cuda):
+    from cmpy_gb300.batched import Batch, BatchGraph
+
+    m = _hub(8, True, inter=4.0, mu=2.0)
+    plans = [m.plan(a, b) for a in range(2, 6) for b in range(2, 6)]
+    b = Batch(plans)
+    ref = b.lanczos(max_steps=200).energy.clone()
+    g = BatchGraph(b, max_steps=200)
+    out = g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out.energy, ref)
+    out2 = g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out2.energy, ref)
+
+
+def test_batch_rejects_non_fixed_point(cuda):
+    from cmpy_gb300.batched import Batch
+    from cmpy_gb300.models import SingleImpurityAndersonModel
+
+    s = SingleImpurityAndersonModel(u=4.0, eps_bath=[-1.3, 0.7], v=[0.31, 0.2])
+    with pytest.raises(ValueError):
+        Batch([s.plan(1, 1)])
