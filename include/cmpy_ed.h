@@ -335,6 +335,17 @@ ED_API ed_status ed_fixed_to_f64(const int64_t* d_xm, int64_t n, int32_t exp, do
 ED_API ed_status ed_matvec_fixed(ed_plan plan, const int64_t* d_xm, int32_t ex, int64_t* d_wm,
                                  int32_t* h_ew, int* h_m_in, ed_stream_t stream);
 
+/* Allocation-free ed_tridiag_lowest (no counterpart in the reference). For callers that
+ * cannot allocate device memory where they need the result — e.g. while one of their streams
+ * is being captured into a CUDA graph, or when their device memory belongs to their own
+ * allocator. The inverse-iteration scratch is a static array of the library's device image
+ * holding 5 * 4096 doubles (160 KB on every GPU that loads the library), so m <= 4096 (larger
+ * m returns ED_ERR_TOO_LARGE). The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and must come before any stream capture on that device. All calls
+ * share the array: calls that overlap on the GPU race on it. Allocates nothing. */
+ED_API ed_status ed_tridiag_lowest_noalloc(const double* d_alpha, const double* d_beta, int m,
+                                           double* d_value, double* d_vec, ed_stream_t stream);
+
 /* ---- Green's functions -------------------------------------------------------------- */
 
 /* Continued fraction G(z) = sign * norm2 / (z' - a0 - b1^2 / (z' - a1 - ...)) with
