@@ -48,7 +48,34 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and adjoint measurements")
+    ap.add_argument("--matvec-only", type=int, default=0,
+                    help="time N fixed-point matvecs of the 14-site sector alone (kernel profiling)")
     return ap.parse_args()
+
+
+def run_matvec_only(n: int):
+    """N integer matvecs of the 14-site (7,7) sector, timed with CUDA events (one JSON line)."""
+    import torch
+
+    from cmpy_gb300 import engine as E
+
+    bonds = [(i, j, T) for i, j in sorted(ring_bonds(N_SITES))]
+    plan = E.Plan.fermion(N_SITES, [-MU] * N_SITES, [U] * N_SITES, bonds, N_UP, N_DN)
+    x = torch.rand(plan.dim, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(5))
+    xm, ex = E.fixed_from_f64(x, plan.fixed_point)
+    wm, _ = plan.matvec_fixed(xm, ex)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * n)]
+    for k in range(n):
+        ev[2 * k].record()
+        plan.matvec_fixed(xm, ex)
+        ev[2 * k + 1].record()
+    torch.cuda.synchronize()
+    us = [ev[2 * k].elapsed_time(ev[2 * k + 1]) * 1e3 for k in range(n)]
+    mean = sum(us) / n
+    print(json.dumps({"kernel": "k_bfp_hub_matvec", "variant": os.environ.get("CMPY_ED_MATVEC", "auto"), "dim": plan.dim, "matvec_us_mean": round(mean, 2),
+                      "matvec_us_min": round(min(us), 2), "gbs": round(16.0 * plan.dim / (mean * 1e-6) / 1e9, 1)}))
 
 
 def peaks():
@@ -295,7 +322,7 @@ def run_ours(args, rank, world, dist):
             "unit": "GB/s",
             "frac": round(achieved / peak, 4) if achieved else None,
             "traffic": traffic,
-            "kernel": "matvec (16*D bytes per launch)",
+            "kernel": "k_bfp_hub_matvec3 (integer H·v, 16*D bytes per launch)",
             "peak_source": f"{peak_kind} (hbm_gbs, burst copy)",
             "matvec_us": round(mv_ms / mv_n * 1e3, 2) if mv_n else None,
         },
@@ -306,9 +333,185 @@ def run_ours(args, rank, world, dist):
     return out
 
 
+def _timed(fn):
+    import torch
+
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    out = fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return out, e0.elapsed_time(e1)
+
+
+def run_batched_sweep():
+    """Batched sweep: all 121 sectors of the 10-site Hubbard ring (t=1, U=6, mu=3) — one persistent
+    batched launch vs per-sector plain launches, same residual tolerance (E0 to 1e-10)."""
+    import torch
+
+    from cmpy_gb300 import engine as E
+    from cmpy_gb300.batched import Batch
+    from cmpy_gb300.models import ChainLattice, HubbardModel
+
+    m = HubbardModel(ChainLattice(10, True), inter=6.0, mu=3.0, hop=1.0)
+    fillings = list(m.basis.iter_fillings())
+    plans = [m.plan(a, b) for a, b in fillings]
+    b = Batch(plans)
+    th, ps, _ = b.tune(40)
+    b.lanczos(max_steps=300, tol=1e-12, check_every=10)  # warm
+    res, t_batch = _timed(lambda: b.lanczos(max_steps=300, tol=1e-12, check_every=10))
+    e_batch = res.energy.cpu().numpy()
+
+    def plain():
+        return [E.lanczos(p, max_steps=min(300, p.dim), want_vector=False, tol=1e-12, check_every=10).energy
+                for p in plans]
+
+    plain()
+    e_plain, t_plain = _timed(plain)
+    e_plain = np.array(e_plain)
+    i = int(np.argmin(e_batch))
+    return {
+        "workload": "hubbard_ring10_U6_all_121_sectors",
+        "batched_ms": round(t_batch, 3),
+        "plain_per_sector_ms": round(t_plain, 3),
+        "speedup": round(t_plain / t_batch, 2),
+        "gs_energy": float(e_batch[i]),
+        "gs_sector": list(fillings[i]),
+        "max_rel_diff_vs_plain": float(np.max(np.abs(e_batch - e_plain) / np.maximum(1.0, np.abs(e_plain)))),
+        "tuned": {"threads": th, "ctas_per_sm": ps},
+        "launches": "1 persistent batched kernel vs per-sector Lanczos sequences",
+    }
+
+
+def run_disorder_batch(n_real: int = 512, n_freq: int = 1024):
+    """Batched disorder: realisations of the 8-site Anderson-Hubbard chain (eps ~ U[-1,1],
+    U=4, t=1, n_up, n_dn ~ U{2..5}); ground state + G(w) at n_freq real frequencies each."""
+    import torch
+
+    from cmpy_gb300.batched import greens_functions_batched
+    from cmpy_gb300.exactdiag import gf_continued_fraction, groundstate_sector
+    from cmpy_gb300.models import ChainLattice, HubbardModel
+
+    rng = np.random.default_rng(2024)
+    lat = ChainLattice(8, False)
+    models = [HubbardModel(lat, inter=4.0, eps=rng.uniform(-1, 1, 8), mu=2.0, hop=1.0) for _ in range(n_real)]
+    sectors = [(int(a), int(b)) for a, b in rng.integers(2, 6, size=(n_real, 2))]
+    # n_freq real frequencies (eta = 0.05) plus 256 Matsubara points at beta = 10: there the
+    # 150-level continued fractions are converged, so batched and per-realisation results must
+    # agree to rounding; on the real axis both are 150-level continued fractions whose
+    # truncation error at eta = 0.05 (up to ~0.3 against the exact Lehmann sum for the largest
+    # sectors) dominates their difference
+    n_mats = 256
+    z = np.concatenate([np.linspace(-8, 8, n_freq) + 0.05j, 1j * (2 * np.arange(n_mats) + 1) * np.pi / 10.0])
+    levels = 150
+    for m_, s_ in zip(models, sectors):  # plans (setup, untimed)
+        for d in (-1, 0, 1):
+            m_.plan(s_[0] + d, s_[1])
+    greens_functions_batched(models[:8], sectors[:8], z, gf_levels=levels)  # warm
+    (eb, gb), t_batch = _timed(lambda: greens_functions_batched(models, sectors, z, gf_levels=levels))
+    n_plain = min(n_real, 64)
+
+    def plain():
+        out = []
+        for m_, (a, b) in zip(models[:n_plain], sectors[:n_plain]):
+            e0, psi = groundstate_sector(m_, a, b, max_steps=300, tol=1e-12)
+            out.append((e0, gf_continued_fraction(m_, z, a, b, e0, psi, n_lev=levels)))
+        return out
+
+    plain()
+    pl, t_plain = _timed(plain)
+    gdiff = max(float(np.max(np.abs(gb[i].cpu().numpy()[:n_freq] - pl[i][1][:n_freq]))) for i in range(n_plain))
+    gdiff_m = max(float(np.max(np.abs(gb[i].cpu().numpy()[n_freq:] - pl[i][1][n_freq:]))) for i in range(n_plain))
+    ediff = max(abs(float(eb[i]) - pl[i][0]) / abs(pl[i][0]) for i in range(n_plain))
+    return {
+        "workload": f"anderson_hubbard_chain8_{n_real}_realisations_gs_gf{n_freq}",
+        "batched_ms": round(t_batch, 3),
+        "plain_ms_extrapolated": round(t_plain * n_real / n_plain, 3),
+        "plain_sample": n_plain,
+        "speedup": round(t_plain * n_real / n_plain / t_batch, 2),
+        "max_rel_energy_diff": ediff,
+        "max_abs_gf_diff_matsubara": gdiff_m,
+        "max_abs_gf_diff_real_axis": gdiff,
+        "n_matsubara": n_mats,
+        "gf_levels": levels,
+    }
+
+
+def run_adjoint(n_siam: int = 2, n_freq: int = 1024):
+    """Adjoint: SIAMs with 1 impurity + 9 bath sites (star), U=4, eps_d=-U/2, sector (5,5);
+    G_imp(i w_n) on n_freq Matsubara frequencies (beta=100) and the adjoint gradient of a
+    least-squares loss against a target hybridisation with 30 poles, w.r.t. bath energies and V."""
+    import torch
+
+    from cmpy_gb300.adjoint import greens_function_ad, siam_parameters
+
+    rng = np.random.default_rng(5)
+    ek = rng.uniform(-2, 2, 30)
+    z = 1j * (2 * np.arange(n_freq) + 1) * np.pi / 100.0
+    gt = torch.as_tensor(1.0 / (z - np.sum(0.3**2 / (z[:, None] - ek[None, :]), axis=1))).cuda()
+    fwd, bwd = [], []
+    for s in range(n_siam):
+        eb = torch.tensor(rng.uniform(-2, 2, 9), dtype=torch.float64, device="cuda", requires_grad=True)
+        v = torch.tensor(rng.uniform(0.1, 0.6, 9), dtype=torch.float64, device="cuda", requires_grad=True)
+        u = torch.tensor(4.0, dtype=torch.float64, device="cuda")
+        theta, n_sites, bonds, width = siam_parameters(u, torch.tensor(0.0, dtype=torch.float64, device="cuda"), eb, v)
+        g, tf = _timed(lambda: greens_function_ad(theta, n_sites, bonds, (5, 5), z, sign_width=width, gs_steps=250,
+                                                   gf_levels=150, ckpt=16))
+        loss = torch.sum(torch.abs(g - gt) ** 2)
+        _, tb = _timed(lambda: loss.backward())
+        fwd.append(tf)
+        bwd.append(tb)
+    return {
+        "workload": f"siam_1p9_sector55_matsubara{n_freq}_beta100",
+        "siams_timed": n_siam,
+        "forward_ms": round(float(np.mean(fwd)), 2),
+        "backward_ms": round(float(np.mean(bwd)), 2),
+        "backward_over_forward": round(float(np.mean(bwd) / np.mean(fwd)), 3),
+    }
+
+
+def run_heisenberg(steps: int = 300):
+    """Heisenberg ring N=20, Sz=0 (D=184,756) with per-bond couplings J_ij = 1 + 0.1*N(0,1)
+    (numpy default_rng(0), bond (i, i+1 mod 20) in order); `steps` Lanczos steps with full
+    reorthogonalisation (CGS2) and the Ritz vector. Vector 1.48 MB: L2-resident, latency bound."""
+    from cmpy_gb300 import engine as E
+    from cmpy_gb300.models import ChainLattice, HeisenbergModel
+
+    n = 20
+    rng = np.random.default_rng(0)
+    J = np.zeros((n, n))
+    for i in range(n):
+        k = (i + 1) % n
+        J[i, k] = J[k, i] = 1.0 + 0.1 * rng.standard_normal()
+    m = HeisenbergModel(ChainLattice(n, True), j=J, jz=J)
+    p = m.plan(0)
+    D = p.dim
+    run = lambda: E.lanczos(p, max_steps=steps, reorth=True, want_vector=True, tol=0.0)  # noqa: E731
+    run()
+    r, t = _timed(run)
+    rp = E.lanczos(p, max_steps=steps, reorth=True, want_vector=True, tol=0.0, profile=True)
+    plain = E.lanczos(p, max_steps=steps, reorth=False, want_vector=False, tol=1e-12, check_every=10)
+    k = r.steps
+    reorth_bytes = sum(2 * 2 * 8 * D * (j + 1) for j in range(k))  # CGS2: 2 passes x (dots + axpy)
+    return {
+        "workload": "heisenberg_ring20_sz0_randomJ_fullreorth",
+        "dim": D,
+        "steps": k,
+        "total_ms": round(t, 3),
+        "ms_per_step": round(t / max(k, 1), 4),
+        "matvec_us": round(1e3 * rp.matvec_ms / max(rp.matvecs, 1), 2),
+        "matvec_gbs": round(16 * D * rp.matvecs / (rp.matvec_ms * 1e-3) / 1e9, 1) if rp.matvec_ms > 0 else None,
+        "reorth_plus_matvec_gbs": round((reorth_bytes + 16 * D * k) / (t * 1e-3) / 1e9, 1),
+        "gs_energy": r.energy,
+        "residual": r.residual,
+        "rel_diff_vs_no_reorth": abs(r.energy - plain.energy) / abs(plain.energy),
+    }
+
+
 def matvec_traffic():
     """DRAM bytes per matvec launch from the committed ncu summary (profiles/), if any."""
-    f = ROOT / "profiles" / "matvec_hubbard14.md"
+    f = ROOT / "profiles" / "k_bfp_hub_matvec3_hubbard14.md"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
@@ -441,6 +644,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
+    if args.matvec_only:
+        run_matvec_only(args.matvec_only)
+        return
     if args.impl == "reference":
         out = run_reference(args, rank, world)
         if out is not None:
@@ -459,6 +665,13 @@ def main():
             out["cpu_baseline"] = cpu_baseline_line()
         else:
             out["cpu_baseline"] = None
+        if not args.no_extras and world == 1:
+            for key, fn in (("batched_sweep", run_batched_sweep), ("batched_disorder", run_disorder_batch),
+                            ("adjoint", run_adjoint), ("heisenberg20", run_heisenberg)):
+                try:
+                    out[key] = fn()
+                except Exception as exc:  # keep the headline line even if an extra fails
+                    out[key] = {"error": f"{type(exc).__name__}: {exc}"}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()

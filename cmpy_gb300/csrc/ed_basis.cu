@@ -25,6 +25,9 @@ ed_status fail(ed_status st, const std::string& msg) {
 
 ed_status cuda_fail(cudaError_t e, const char* what) {
   g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  // A non-sticky error (bad launch configuration, invalid attribute) stays in the runtime's
+  // per-thread error slot and would be reported again by the next launch check: clear it.
+  (void)cudaGetLastError();
   return ED_ERR_CUDA;
 }
 
@@ -48,6 +51,7 @@ ed_status device_context(DeviceContext** out) {
     DeviceContext* c = new DeviceContext();
     c->device = dev;
     cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaDeviceGetAttribute"); }
     std::vector<uint64_t> tab(64 * 64);
     for (int n = 0; n < 64; ++n)

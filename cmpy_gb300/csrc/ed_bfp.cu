@@ -296,6 +296,496 @@ __global__ void __launch_bounds__(NT) k_bfp_hub_matvec(BfpHubArgs a, const int64
   }
 }
 
+// ---- matvec v2: one 1024-thread CTA per SM, dn table resident in shared memory ----------------
+// Each CTA keeps the whole dn slot table (max_dn x nd/2 packed slot pairs) in shared memory for
+// its lifetime and processes MR target rows per iteration, so each table word serves MR rows.
+// The input X is read with an L2 evict_last policy (every row is re-read by ~8 target rows) and
+// W is written with evict_first, so the streaming output does not push X out of L2.
+constexpr int MV2_NT = 1024;
+constexpr int MV2_R = 2;
+// the kernel's static shared memory (two warp-partial arrays) plus slack
+constexpr size_t MV2_STATIC_SMEM = 2 * (MV2_NT / 32) * 8 + 512;
+
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ longlong2 ld2_keep(const int64_t* p, uint64_t pol) {
+  longlong2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.s64 {%0, %1}, [%2], %3;"
+               : "=l"(v.x), "=l"(v.y)
+               : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st2_stream(int64_t* p, int64_t a, int64_t b, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.s64 [%0], {%1, %2}, %3;" ::"l"(p), "l"(a), "l"(b), "l"(pol) : "memory");
+}
+
+template <bool DIAG64>
+__global__ void __launch_bounds__(MV2_NT, 1) k_bfp_hub_matvec2(BfpHubArgs a, const int64_t* __restrict__ X,
+                                                              int64_t* __restrict__ W, double* partial,
+                                                              unsigned long long* partial_max, BfpState* st) {
+  if (st && *(volatile int*)&st->stop) return;
+  extern __shared__ int64_t smem[];
+  __shared__ double smd[MV2_NT / 32];
+  __shared__ unsigned long long smu[MV2_NT / 32];
+  const int64_t nd = a.nd;
+  const int np = (int)(nd / 2);                       // column pairs
+  const int xstride = (int)(2 * nd + 2);              // +/- row copy and a zero slot, 16-byte aligned
+  int64_t* xs = smem;                                 // [MV2_R][xstride]
+  uint32_t* tab = (uint32_t*)(smem + MV2_R * xstride);  // [max_dn][np]
+  const uint32_t* gtab = (const uint32_t*)a.dn_tab;
+  for (int i = threadIdx.x; i < a.max_dn * np; i += MV2_NT) tab[i] = __ldg(gtab + i);
+  for (int r = threadIdx.x; r < MV2_R; r += MV2_NT) { xs[r * xstride + 2 * nd] = 0; xs[r * xstride + 2 * nd + 1] = 0; }
+  const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
+  I128 dot{0, 0};
+  unsigned long long mx = 0;
+  for (int64_t row0 = (int64_t)blockIdx.x * MV2_R; row0 < a.nu; row0 += (int64_t)gridDim.x * MV2_R) {
+    const int nr = (int)min((int64_t)MV2_R, a.nu - row0);
+    __syncthreads();
+    for (int r = 0; r < nr; ++r) {
+      const int64_t* xrow = X + (row0 + r) * nd;
+      int64_t* xr = xs + r * xstride;
+      for (int p = threadIdx.x; p < np; p += MV2_NT) {
+        const longlong2 v = ld2_keep(xrow + 2 * p, keep);
+        *(longlong2*)(xr + 2 * p) = v;
+        *(longlong2*)(xr + nd + 2 * p) = make_longlong2(-v.x, -v.y);
+      }
+    }
+    __syncthreads();
+    int32_t o0[MV2_R], o1[MV2_R], op[MV2_R];
+    uint64_t su[MV2_R];
+    int64_t eu[MV2_R], eu64[MV2_R];
+#pragma unroll
+    for (int r = 0; r < MV2_R; ++r) {
+      const int64_t row = r < nr ? row0 + r : row0;
+      o0[r] = __ldg(a.up_off + row);
+      o1[r] = r < nr ? __ldg(a.up_off + row + 1) : o0[r];
+      op[r] = r < nr ? o0[r] + __ldg(a.up_npos + row) : o0[r];
+      su[r] = __ldg(a.up_states + row);
+      eu[r] = DIAG64 ? 0 : (int64_t)__ldg(a.e_up + row);
+      eu64[r] = DIAG64 ? __ldg(a.e_up_fx + row) : 0;
+    }
+    for (int p = threadIdx.x; p < np; p += MV2_NT) {
+      const int64_t d = 2 * p;
+      int64_t h0[MV2_R], h1[MV2_R];
+#pragma unroll
+      for (int r = 0; r < MV2_R; ++r) {
+        h0[r] = 0;
+        h1[r] = 0;
+        // four independent row loads in flight per iteration (memory-level parallelism)
+        int32_t e = o0[r];
+        for (; e + 4 <= op[r]; e += 4) {
+          longlong2 v[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) v[q] = ld2_keep(X + (int64_t)__ldg(a.up_idx + e + q) * nd + d, keep);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) { h0[r] += v[q].x; h1[r] += v[q].y; }
+        }
+        for (; e < op[r]; ++e) {
+          const longlong2 v = ld2_keep(X + (int64_t)__ldg(a.up_idx + e) * nd + d, keep);
+          h0[r] += v.x;
+          h1[r] += v.y;
+        }
+        for (; e + 4 <= o1[r]; e += 4) {
+          longlong2 v[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) v[q] = ld2_keep(X + (int64_t)__ldg(a.up_idx + e + q) * nd + d, keep);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) { h0[r] -= v[q].x; h1[r] -= v[q].y; }
+        }
+        for (; e < o1[r]; ++e) {
+          const longlong2 v = ld2_keep(X + (int64_t)__ldg(a.up_idx + e) * nd + d, keep);
+          h0[r] -= v.x;
+          h1[r] -= v.y;
+        }
+      }
+      for (int e = 0; e < a.max_dn; ++e) {
+        const uint32_t sl = tab[e * np + p];
+        const int s0 = (int)(sl & 0xFFFFu), s1 = (int)(sl >> 16);
+#pragma unroll
+        for (int r = 0; r < MV2_R; ++r) {
+          h0[r] += xs[r * xstride + s0];
+          h1[r] += xs[r * xstride + s1];
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < MV2_R; ++r) {
+        if (r < nr) {
+          const int64_t x0 = xs[r * xstride + d], x1 = xs[r * xstride + d + 1];
+          const int64_t w0 = (int64_t)a.t_int * h0[r] + bfp_diag_term<DIAG64>(a, eu[r], eu64[r], su[r], d, x0);
+          const int64_t w1 = (int64_t)a.t_int * h1[r] + bfp_diag_term<DIAG64>(a, eu[r], eu64[r], su[r], d + 1, x1);
+          st2_stream(W + (row0 + r) * nd + d, w0, w1, stream);
+          add128(dot, mul_s64(x0, w0));
+          add128(dot, mul_s64(x1, w1));
+          mx = max(mx, max(uabs64(w0), uabs64(w1)));
+        }
+      }
+    }
+  }
+  if (!partial) return;
+  const double s = block_sum<MV2_NT>(i128_to_double(dot), smd);
+  const unsigned long long m = block_max_u64<MV2_NT>(mx, smu);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = s;
+    partial_max[blockIdx.x] = m;
+  }
+}
+
+// ---- matvec v3: bulk-copied rows, interleaved row pair, bond-major dn gathers -------------------
+// One persistent CTA per SM walks groups of MV3_R = 2 target rows. A bulk copy (cp.async.bulk,
+// completion on an mbarrier) brings the two rows of the NEXT group into a landing buffer while
+// the CTA computes the current group from an interleaved copy xs2[c] = (row0[c], row1[c]), so one
+// 16-byte shared load gathers a dn partner for both rows. Each thread owns columns
+// c = tid + j*blockDim (lane-contiguous), so the gathers of one bond read nearly contiguous
+// partner columns; one 32-bit table word holds the partner slots of two bonds.
+// Up-neighbour rows stream from L2 (coalesced 8-byte loads, evict_last policy), eight loads in
+// flight per thread; the neighbour lists are padded to multiples of 8 with the target row itself
+// and the padding is subtracted once (exact integer arithmetic).
+constexpr int MV3_R = 2;
+constexpr int MV3_MAXNT = 896;  // 28 warps: up to 72 registers per thread with one CTA per SM
+constexpr size_t MV3_STATIC_SMEM = 2 * (MV3_MAXNT / 32) * 8 + 512;
+constexpr long MV3_WAIT_LIMIT = 1L << 22;  // bounded mbarrier polls before giving up
+
+struct Mv3Layout {
+  int lstride;  // int32 per staged up-list of one row: + segment, - segment, each padded to 4
+  size_t raw_off, xs_off, tab_off, lst_off, cnt_off, bar_off, total;
+};
+
+__host__ __device__ inline Mv3Layout mv3_layout(int64_t nd, int n_b2, int max_up) {
+  auto al = [](size_t v) { return (v + 127) & ~(size_t)127; };
+  Mv3Layout L;
+  L.lstride = ((max_up + 3) & ~3) + 4;
+  L.raw_off = 0;                                                   // [MV3_R][nd] landing rows
+  L.xs_off = al(L.raw_off + (size_t)MV3_R * nd * 8);               // [nd + 1][MV3_R] interleaved
+  L.tab_off = al(L.xs_off + (size_t)(nd + 1) * MV3_R * 8);         // [n_b2][nd] slot pairs
+  L.lst_off = al(L.tab_off + (size_t)n_b2 * nd * 4);               // [2][MV3_R][lstride]
+  L.cnt_off = al(L.lst_off + (size_t)2 * MV3_R * L.lstride * 4);   // [2][MV3_R][4]
+  L.bar_off = al(L.cnt_off + (size_t)2 * MV3_R * 4 * 4);
+  L.total = L.bar_off + 8;
+  return L;
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait for phase `parity` of an mbarrier; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+  for (long it = 0; it < MV3_WAIT_LIMIT; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// global -> shared bulk copy (16-byte aligned, size a multiple of 16), completes on `bar`
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar, uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+      : "memory");
+}
+// read-only data (X is not written while the kernel runs), so the asm is not volatile: the
+// compiler may batch these loads
+__device__ __forceinline__ int64_t ld_keep(const int64_t* p, uint64_t pol) {
+  int64_t v;
+  asm("ld.global.nc.L2::cache_hint.s64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_stream(int64_t* p, int64_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.s64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+
+// block reductions for a runtime block size (a multiple of 32, at most MV3_MAXNT)
+__device__ __forceinline__ double block_sum_rt(double v, double* sm) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (l == 0) sm[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (l < nw) ? sm[l] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+  }
+  return r;
+}
+__device__ __forceinline__ unsigned long long block_max_rt(unsigned long long v, unsigned long long* sm) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (l == 0) sm[w] = v;
+  __syncthreads();
+  unsigned long long r = 0;
+  if (w == 0) {
+    r = (l < nw) ? sm[l] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r = max(r, __shfl_xor_sync(0xffffffffu, r, o));
+  }
+  return r;
+}
+
+// diagonal term of one element with the column's data already loaded
+template <bool DIAG64>
+__device__ __forceinline__ int64_t bfp_diag_col(const BfpHubArgs& a, int64_t row_e32, int64_t row_e64, uint64_t su,
+                                                uint64_t sd, int32_t ed32, int64_t ed64, int64_t x) {
+  const uint64_t both = su & sd;
+  if (!DIAG64) {
+    const int32_t dg = (int32_t)row_e32 + ed32 + bfp_uterm(a, both);
+    return (int64_t)dg * x;
+  } else {
+    const int64_t dg = row_e64 + ed64 + bfp_uterm64(a, both);
+    return shr128_round(mul_s64(dg, x), a.dshift);
+  }
+}
+
+__device__ __forceinline__ longlong2 ld2_keep_nv(const int64_t* p, uint64_t pol) {
+  longlong2 v;
+  asm("ld.global.nc.L2::cache_hint.v2.s64 {%0, %1}, [%2], %3;" : "=l"(v.x), "=l"(v.y) : "l"(p), "l"(pol));
+  return v;
+}
+// four 16-byte row loads (two adjacent columns) of the list entries lst[0..4), summed
+__device__ __forceinline__ longlong2 sum4x2(const int64_t* xc, const int32_t* lst, uint64_t pol) {
+  const int4 i = *(const int4*)lst;
+  const longlong2 v0 = ld2_keep_nv(xc + i.x, pol), v1 = ld2_keep_nv(xc + i.y, pol), v2 = ld2_keep_nv(xc + i.z, pol),
+                  v3 = ld2_keep_nv(xc + i.w, pol);
+  return make_longlong2((v0.x + v1.x) + (v2.x + v3.x), (v0.y + v1.y) + (v2.y + v3.y));
+}
+// 64-bit warp shuffle
+__device__ __forceinline__ int64_t shfl64(int64_t v, int src) {
+  return (int64_t)__shfl_sync(0xffffffffu, (long long)v, src);
+}
+
+template <bool DIAG64>
+__global__ void __launch_bounds__(MV3_MAXNT, 1)
+    k_bfp_hub_matvec3(BfpHubArgs a, const uint32_t* __restrict__ btab2, int n_b2, int n_b2pos, int max_up,
+                      const int64_t* __restrict__ X, int64_t* __restrict__ W, double* partial,
+                      unsigned long long* partial_max, BfpState* st, int* status) {
+  if (st && *(volatile int*)&st->stop) return;
+  extern __shared__ __align__(128) unsigned char sm3[];
+  __shared__ double smd[MV3_MAXNT / 32];
+  __shared__ unsigned long long smu[MV3_MAXNT / 32];
+  const int64_t nd = a.nd, nu = a.nu;
+  const Mv3Layout L = mv3_layout(nd, n_b2, max_up);
+  int64_t* raw = (int64_t*)(sm3 + L.raw_off);          // [MV3_R][nd]
+  longlong2* xs2 = (longlong2*)(sm3 + L.xs_off);       // [nd + 1]
+  uint32_t* tab = (uint32_t*)(sm3 + L.tab_off);        // [n_b2][nd]
+  int32_t* lst = (int32_t*)(sm3 + L.lst_off);          // [2][MV3_R][lstride]
+  int32_t* cnt = (int32_t*)(sm3 + L.cnt_off);          // [2][MV3_R][4]: + len, - len, pad correction
+  uint64_t* bar = (uint64_t*)(sm3 + L.bar_off);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int64_t ngroups = (nu + MV3_R - 1) / MV3_R;
+  const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
+  const unsigned row_bytes = (unsigned)(nd * 8);
+
+  // stage group g: its padded up-lists into list buffer s (element offsets of neighbour rows;
+  // padding = the target row) and, from thread 0, the bulk copies of its rows into `raw`
+  auto stage = [&](int64_t g, int s) {
+    const int64_t u0 = g * MV3_R;
+    const int nr = (int)min((int64_t)MV3_R, nu - u0);
+    for (int t = tid; t < MV3_R * L.lstride; t += nt) {
+      const int r = t / L.lstride, e = t - r * L.lstride;
+      if (r >= nr) continue;
+      const int64_t u = u0 + r;
+      const int32_t o0 = __ldg(a.up_off + u), n = __ldg(a.up_off + u + 1) - o0, np = __ldg(a.up_npos + u);
+      const int32_t cp = (np + 3) & ~3, cn = ((n - np) + 3) & ~3;
+      int32_t v = (int32_t)(u * nd);
+      if (e < cp) {
+        if (e < np) v = __ldg(a.up_idx + o0 + e) * (int32_t)nd;
+      } else if (e < cp + cn) {
+        if (e - cp < n - np) v = __ldg(a.up_idx + o0 + np + (e - cp)) * (int32_t)nd;
+      }
+      lst[(s * MV3_R + r) * L.lstride + e] = v;
+    }
+    for (int r = tid; r < MV3_R; r += nt) {
+      int32_t cp = 0, cn = 0, corr = 0;
+      if (r < nr) {
+        const int64_t u = u0 + r;
+        const int32_t n = __ldg(a.up_off + u + 1) - __ldg(a.up_off + u), np = __ldg(a.up_npos + u);
+        cp = (np + 3) & ~3;
+        cn = ((n - np) + 3) & ~3;
+        corr = (cn - (n - np)) - (cp - np);  // padding copies of the target row, with sign
+      }
+      cnt[(s * MV3_R + r) * 4 + 0] = cp;
+      cnt[(s * MV3_R + r) * 4 + 1] = cn;
+      cnt[(s * MV3_R + r) * 4 + 2] = corr;
+    }
+    if (tid == 0) {
+      mbar_expect_tx(bar, row_bytes * nr);
+      for (int r = 0; r < nr; ++r) bulk_g2s(raw + (size_t)r * nd, X + (u0 + r) * nd, row_bytes, bar, keep);
+    }
+  };
+
+  // one-time set-up: the table, the zero slot pair, the barrier
+  {
+    for (int64_t i = tid; i < (int64_t)n_b2 * nd; i += nt) tab[i] = __ldg(btab2 + i);
+    if (tid == 0) {
+      xs2[nd] = make_longlong2(0, 0);
+      mbar_init(bar, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+  }
+  bool pending = false;  // a bulk copy into `raw` has been issued and not yet waited for
+  unsigned par = 0u;     // parity of the barrier's next phase completion
+  if ((int64_t)blockIdx.x < ngroups) {
+    stage(blockIdx.x, 0);
+    pending = true;
+  }
+  __syncthreads();
+
+  I128 dot{0, 0};
+  unsigned long long mx = 0;
+  bool bad = false;
+  int k = 0;
+  for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x, ++k) {
+    const int s = k & 1;
+    const int64_t row0 = g * MV3_R;
+    const int nr = (int)min((int64_t)MV3_R, nu - row0);
+    if (mbar_wait_bounded(bar, par)) {
+      pending = false;
+      par ^= 1u;
+    } else {
+      bad = true;
+    }
+    if (__syncthreads_or(bad)) {
+      bad = true;
+      break;
+    }
+    // interleave the landed rows (a missing second row reads as zeros)
+    for (int64_t c = tid; c < nd; c += nt) xs2[c] = make_longlong2(raw[c], nr > 1 ? raw[nd + c] : 0);
+    __syncthreads();  // xs2 complete; raw free for the next group's copy
+    const int64_t gn = g + gridDim.x;
+    if (gn < ngroups) {
+      stage(gn, s ^ 1);  // list buffer s^1 was released by the barrier that ended step k-1
+      pending = true;
+    }
+    const int32_t* l0 = lst + (s * MV3_R + 0) * L.lstride;
+    const int32_t* l1 = lst + (s * MV3_R + 1) * L.lstride;
+    const int32_t cp0 = cnt[(s * MV3_R + 0) * 4 + 0], cn0 = cnt[(s * MV3_R + 0) * 4 + 1];
+    const int32_t cp1 = cnt[(s * MV3_R + 1) * 4 + 0], cn1 = cnt[(s * MV3_R + 1) * 4 + 1];
+    const int64_t corr0 = cnt[(s * MV3_R + 0) * 4 + 2], corr1 = cnt[(s * MV3_R + 1) * 4 + 2];
+    const uint64_t su0 = __ldg(a.up_states + row0), su1 = __ldg(a.up_states + row0 + (nr > 1 ? 1 : 0));
+    const int64_t eu0 = DIAG64 ? 0 : (int64_t)__ldg(a.e_up + row0);
+    const int64_t eu1 = DIAG64 ? 0 : (int64_t)__ldg(a.e_up + row0 + (nr > 1 ? 1 : 0));
+    const int64_t ef0 = DIAG64 ? __ldg(a.e_up_fx + row0) : 0;
+    const int64_t ef1 = DIAG64 ? __ldg(a.e_up_fx + row0 + (nr > 1 ? 1 : 0)) : 0;
+    const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+    const int n0 = cp0 + cn0, n1 = cp1 + cn1, nmax = max(n0, n1);
+    // warps take 64-column chunks; lane l owns columns base + l and base + 32 + l
+    for (int64_t base = (int64_t)warp * 64; base < nd; base += (int64_t)nwarp * 64) {
+      // the chunk's per-column data, requested early
+      const int64_t c_lo = min(base + lane, nd - 1), c_hi = min(base + 32 + lane, nd - 1);
+      const uint64_t sd_lo = __ldg(a.dn_states + c_lo), sd_hi = __ldg(a.dn_states + c_hi);
+      const int32_t e32_lo = DIAG64 ? 0 : __ldg(a.e_dn + c_lo), e32_hi = DIAG64 ? 0 : __ldg(a.e_dn + c_hi);
+      const int64_t e64_lo = DIAG64 ? __ldg(a.e_dn_fx + c_lo) : 0, e64_hi = DIAG64 ? __ldg(a.e_dn_fx + c_hi) : 0;
+      // up neighbours in pair layout: lane l loads columns base + 2l, base + 2l + 1 (16 bytes)
+      const int64_t cpair = base + 2 * lane;
+      const int64_t* xc = X + min(cpair, nd - 2);  // out-of-range lanes load a valid pair, unused
+      longlong2 u0 = make_longlong2(0, 0), u1 = make_longlong2(0, 0);
+      for (int e = 0; e < nmax; e += 4) {
+        if (e < n0) {
+          const longlong2 t = sum4x2(xc, l0 + e, keep);
+          if (e < cp0) { u0.x += t.x; u0.y += t.y; } else { u0.x -= t.x; u0.y -= t.y; }
+        }
+        if (e < n1) {
+          const longlong2 t = sum4x2(xc, l1 + e, keep);
+          if (e < cp1) { u1.x += t.x; u1.y += t.y; } else { u1.x -= t.x; u1.y -= t.y; }
+        }
+      }
+      // to the lane-contiguous layout: column base + l sits in lane l/2 (element l&1),
+      // column base + 32 + l in lane 16 + l/2
+      const bool odd = lane & 1;
+      int64_t up_lo[2], up_hi[2];
+      {
+        const int s_lo = lane >> 1, s_hi = 16 + (lane >> 1);
+        const int64_t a0 = shfl64(u0.x, s_lo), b0 = shfl64(u0.y, s_lo), a1 = shfl64(u1.x, s_lo), b1 = shfl64(u1.y, s_lo);
+        const int64_t c0 = shfl64(u0.x, s_hi), d0 = shfl64(u0.y, s_hi), c1 = shfl64(u1.x, s_hi), d1 = shfl64(u1.y, s_hi);
+        up_lo[0] = odd ? b0 : a0;
+        up_lo[1] = odd ? b1 : a1;
+        up_hi[0] = odd ? d0 : c0;
+        up_hi[1] = odd ? d1 : c1;
+      }
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int64_t c = base + 32 * half + lane;
+        if (c >= nd) continue;
+        const longlong2 xo = xs2[c];
+        int64_t h0 = corr0 * xo.x + (half ? up_hi[0] : up_lo[0]);
+        int64_t h1 = corr1 * xo.y + (half ? up_hi[1] : up_lo[1]);
+        // dn neighbours: two bonds per table word, + rows then - rows; slot nd reads zeros
+        const uint32_t* tc = tab + c;
+        for (int p = 0; p < n_b2pos; ++p) {
+          const uint32_t w = tc[(int64_t)p * nd];
+          const longlong2 va = xs2[w & 0xffffu], vb = xs2[w >> 16];
+          h0 += va.x + vb.x;
+          h1 += va.y + vb.y;
+        }
+        for (int p = n_b2pos; p < n_b2; ++p) {
+          const uint32_t w = tc[(int64_t)p * nd];
+          const longlong2 va = xs2[w & 0xffffu], vb = xs2[w >> 16];
+          h0 -= va.x + vb.x;
+          h1 -= va.y + vb.y;
+        }
+        const uint64_t sd = half ? sd_hi : sd_lo;
+        const int32_t ed32 = half ? e32_hi : e32_lo;
+        const int64_t ed64 = half ? e64_hi : e64_lo;
+        {
+          const int64_t w0 = (int64_t)a.t_int * h0 + bfp_diag_col<DIAG64>(a, eu0, ef0, su0, sd, ed32, ed64, xo.x);
+          st_stream(W + row0 * nd + c, w0, stream);
+          add128(dot, mul_s64(xo.x, w0));
+          mx = max(mx, uabs64(w0));
+        }
+        if (nr > 1) {
+          const int64_t w1 = (int64_t)a.t_int * h1 + bfp_diag_col<DIAG64>(a, eu1, ef1, su1, sd, ed32, ed64, xo.y);
+          st_stream(W + (row0 + 1) * nd + c, w1, stream);
+          add128(dot, mul_s64(xo.y, w1));
+          mx = max(mx, uabs64(w1));
+        }
+      }
+    }
+    __syncthreads();  // xs2 and list buffer s free
+  }
+  if (bad) {
+    // a wait ran out: record it, let a copy still in flight land (bounded), leave
+    if (tid == 0) {
+      record_status(status, DEV_TIMEOUT);
+      if (st) *(volatile int*)&st->stop = 3;  // later kernels of the solve return at once
+      if (pending) (void)mbar_wait_bounded(bar, par);
+    }
+    __syncthreads();
+    return;
+  }
+  if (!partial) return;
+  const double sdot = block_sum_rt(i128_to_double(dot), smd);
+  const unsigned long long m = block_max_rt(mx, smu);
+  if (tid == 0) {
+    partial[blockIdx.x] = sdot;
+    partial_max[blockIdx.x] = m;
+  }
+}
+
 // Lanczos scalars after the matvec of step k (single block, runs after the matvec):
 //   alpha_k = <R_k, W> / beta_k^2 ;  R_{k+1} = c_w W + c_q R_k + c_p R_{k-1}
 //   c_w = 1/beta_k, c_q = -alpha_k/beta_k, c_p = -beta_k/beta_{k-1}
@@ -341,28 +831,71 @@ __global__ void k_bfp_scalars(BfpVecs v, int k, int F, int m_in, const double* p
   v.eR[k + 1] = er;
 }
 
-// R_{k+1} = round((A_w W + A_q R_k + A_p R_{k-1}) / 2^SA); ||R_{k+1}||^2 and max -> beta[k+1]
-__global__ void k_bfp_update(BfpVecs v, int k, const int64_t* __restrict__ W, double* partial,
-                             unsigned long long* partial_max, double* beta, const double* alpha, BfpState* st,
-                             int final_k) {
+// one element of the three-term update, with the running exact norm and max
+__device__ __forceinline__ int64_t bfp_upd1(int64_t Aw, int64_t Aq, int64_t Ap, int SA, int64_t w, int64_t q,
+                                            int64_t pv, I128& nrm, unsigned long long& mx) {
+  I128 s = mul_s64(Aw, w);
+  add128(s, mul_s64(Aq, q));
+  add128(s, mul_s64(Ap, pv));
+  const int64_t r = shr128_round(s, SA);
+  add128(nrm, mul_s64(r, r));
+  mx = max(mx, uabs64(r));
+  return r;
+}
+__device__ __forceinline__ longlong2 ld2_stream(const int64_t* p, uint64_t pol) {
+  longlong2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.s64 {%0, %1}, [%2], %3;" : "=l"(v.x), "=l"(v.y) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st2_keep(int64_t* p, int64_t a, int64_t b, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.s64 [%0], {%1, %2}, %3;" ::"l"(p), "l"(a), "l"(b), "l"(pol) : "memory");
+}
+
+// R_{k+1} = round((A_w W + A_q R_k + A_p R_{k-1}) / 2^SA); ||R_{k+1}||^2 and max -> beta[k+1].
+// VEC (D even, 16-byte aligned vectors): element pairs, two pairs per thread in flight; the
+// inputs are read with an L2 evict_first policy and R_{k+1} is written with evict_last, so the
+// next matvec finds its input in L2.
+template <bool VEC>
+__global__ void __launch_bounds__(BT, 4) k_bfp_update(BfpVecs v, int k, const int64_t* __restrict__ W, double* partial,
+                                                   unsigned long long* partial_max, double* beta,
+                                                   const double* alpha, BfpState* st, int final_k) {
   if (*(volatile int*)&st->stop) return;
   __shared__ double sm[BT / 32];
   __shared__ unsigned long long smu[BT / 32];
-  const int64_t Aw = st->A_w, Aq = st->A_q, Ap = st->A_p;
+  const int64_t Aw = st->A_w, Aq = st->A_q, Ap = k > 0 ? st->A_p : 0;
   const int SA = st->SA;
   const int64_t* __restrict__ rq = v.vec(k);
-  const int64_t* __restrict__ rp = k > 0 ? v.vec(k - 1) : nullptr;
+  // k = 0: no R_{k-1}; read R_k again with a zero coefficient (keeps the loop branch-free)
+  const int64_t* __restrict__ rp = k > 0 ? v.vec(k - 1) : rq;
   int64_t* __restrict__ rn = v.vec(k + 1);
   I128 nrm{0, 0};
   unsigned long long mx = 0;
-  for (int64_t i = blockIdx.x * (int64_t)BT + threadIdx.x; i < v.D; i += (int64_t)gridDim.x * BT) {
-    I128 s = mul_s64(Aw, W[i]);
-    add128(s, mul_s64(Aq, rq[i]));
-    if (rp) add128(s, mul_s64(Ap, rp[i]));
-    const int64_t r = shr128_round(s, SA);
-    rn[i] = r;
-    add128(nrm, mul_s64(r, r));
-    mx = max(mx, uabs64(r));
+  if (VEC) {
+    const uint64_t first = policy_evict_first(), last = policy_evict_last();
+    const int64_t P = v.D >> 1, stride = (int64_t)gridDim.x * BT;
+    int64_t i = blockIdx.x * (int64_t)BT + threadIdx.x;
+    for (; i + stride < P; i += 2 * stride) {
+      const int64_t j0 = 2 * i, j1 = 2 * (i + stride);
+      const longlong2 w0 = ld2_stream(W + j0, first), w1 = ld2_stream(W + j1, first);
+      const longlong2 q0 = ld2_stream(rq + j0, first), q1 = ld2_stream(rq + j1, first);
+      const longlong2 p0 = ld2_stream(rp + j0, first), p1 = ld2_stream(rp + j1, first);
+      const int64_t a0 = bfp_upd1(Aw, Aq, Ap, SA, w0.x, q0.x, p0.x, nrm, mx);
+      const int64_t a1 = bfp_upd1(Aw, Aq, Ap, SA, w0.y, q0.y, p0.y, nrm, mx);
+      const int64_t b0 = bfp_upd1(Aw, Aq, Ap, SA, w1.x, q1.x, p1.x, nrm, mx);
+      const int64_t b1 = bfp_upd1(Aw, Aq, Ap, SA, w1.y, q1.y, p1.y, nrm, mx);
+      st2_keep(rn + j0, a0, a1, last);
+      st2_keep(rn + j1, b0, b1, last);
+    }
+    for (; i < P; i += stride) {
+      const int64_t j0 = 2 * i;
+      const longlong2 w0 = ld2_stream(W + j0, first), q0 = ld2_stream(rq + j0, first), p0 = ld2_stream(rp + j0, first);
+      const int64_t a0 = bfp_upd1(Aw, Aq, Ap, SA, w0.x, q0.x, p0.x, nrm, mx);
+      const int64_t a1 = bfp_upd1(Aw, Aq, Ap, SA, w0.y, q0.y, p0.y, nrm, mx);
+      st2_keep(rn + j0, a0, a1, last);
+    }
+  } else {
+    for (int64_t i = blockIdx.x * (int64_t)BT + threadIdx.x; i < v.D; i += (int64_t)gridDim.x * BT)
+      rn[i] = bfp_upd1(Aw, Aq, Ap, SA, W[i], rq[i], rp[i], nrm, mx);
   }
   const double s = block_sum<BT>(i128_to_double(nrm), sm);
   const unsigned long long m = block_max_u64<BT>(mx, smu);
@@ -468,6 +1001,7 @@ ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
   // row tables (host copies of the FP64 tables)
   std::vector<int32_t> uoff(p->num_up + 1), uidx(p->up.nnz), doff(p->num_dn + 1), didx(p->dn.nnz);
   std::vector<double> ucoef(p->up.nnz), dcoef(p->dn.nnz);
+  std::vector<int16_t> dbond(p->dn.nnz);
   ED_CUDA(cudaMemcpyAsync(uoff.data(), p->up.off, uoff.size() * 4, cudaMemcpyDeviceToHost, s));
   ED_CUDA(cudaMemcpyAsync(doff.data(), p->dn.off, doff.size() * 4, cudaMemcpyDeviceToHost, s));
   if (p->up.nnz) {
@@ -477,6 +1011,7 @@ ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
   if (p->dn.nnz) {
     ED_CUDA(cudaMemcpyAsync(didx.data(), p->dn.idx, didx.size() * 4, cudaMemcpyDeviceToHost, s));
     ED_CUDA(cudaMemcpyAsync(dcoef.data(), p->dn.coef, dcoef.size() * 8, cudaMemcpyDeviceToHost, s));
+    ED_CUDA(cudaMemcpyAsync(dbond.data(), p->dn.bond, dbond.size() * 2, cudaMemcpyDeviceToHost, s));
   }
   ED_CUDA(cudaStreamSynchronize(s));
   const int64_t nu = p->num_up, nd = p->num_dn;
@@ -509,6 +1044,41 @@ ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
       ++e;
     }
   }
+  // bond-major table: one row per (bond, sign) pair that occurs, + rows first, so that a warp
+  // of consecutive columns gathers partners of one bond (nearly contiguous addresses)
+  std::vector<int> brow(2 * ED_MAX_BONDS, -1);
+  int n_bpos = 0, n_bt = 0;
+  for (int sg = 0; sg < 2; ++sg) {
+    for (size_t k = 0; k < dcoef.size(); ++k) {
+      if (dcoef[k] == 0.0 || (dcoef[k] < 0.0) != (sg == 1)) continue;
+      const int key = 2 * dbond[k] + sg;
+      if (brow[key] < 0) brow[key] = n_bt++;
+    }
+    if (sg == 0) n_bpos = n_bt;
+  }
+  // renumber so that rows follow bond order within each sign class
+  {
+    int nxt = 0;
+    for (int sg = 0; sg < 2; ++sg)
+      for (int b = 0; b < ED_MAX_BONDS; ++b)
+        if (brow[2 * b + sg] >= 0) brow[2 * b + sg] = nxt++;
+  }
+  // padded row numbers: + rows [0, pos_pad), - rows [pos_pad, pos_pad + neg_pad)
+  const int pos_pad = n_bpos + (n_bpos & 1), n_neg = n_bt - n_bpos, neg_pad = n_neg + (n_neg & 1);
+  const int n_rows = pos_pad + neg_pad;
+  std::vector<uint16_t> btab((size_t)std::max(n_rows, 2) * nd, (uint16_t)nd);
+  for (int64_t c = 0; c < nd; ++c)
+    for (int32_t k = doff[c]; k < doff[c + 1]; ++k) {
+      if (dcoef[k] == 0.0) continue;
+      int row = brow[2 * dbond[k] + (dcoef[k] < 0.0 ? 1 : 0)];
+      if (row >= n_bpos) row += pos_pad - n_bpos;
+      btab[(size_t)row * nd + c] = (uint16_t)didx[k];
+    }
+  std::vector<uint32_t> btab2((size_t)std::max(n_rows / 2, 1) * nd);
+  for (int pr = 0; pr < std::max(n_rows / 2, 1); ++pr)
+    for (int64_t c = 0; c < nd; ++c)
+      btab2[(size_t)pr * nd + c] = (uint32_t)btab[(size_t)(2 * pr) * nd + c] |
+                                   ((uint32_t)btab[(size_t)(2 * pr + 1) * nd + c] << 16);
   // diagonal bound in units of 2^-F, and the overflow guard
   //   |W| <= (max|diag| 2^F + hops * t_int) * 2^m_in < 2^62
   B.u_uniform = p->fp.u_uniform;
@@ -563,6 +1133,10 @@ ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
   ED_TRY(up(&B.up_npos, bnpos.data(), bnpos.size() * 4));
   ED_TRY(up(&B.up_idx, bidx.data(), bidx.size() * 4));
   ED_TRY(up(&B.dn_tab, tab.data(), tab.size() * 2));
+  ED_TRY(up(&B.dn_btab2, btab2.data(), btab2.size() * 4));
+  B.n_b2 = n_rows / 2;
+  B.n_b2pos = pos_pad / 2;
+  B.max_up = max_up;
   if (!diag64) {
     ED_TRY(up(&B.e_up_int, eui.data(), eui.size() * 4));
     ED_TRY(up(&B.e_dn_int, edi.data(), edi.size() * 4));
@@ -577,7 +1151,7 @@ ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
 
 void free_bfp(ed_plan_s* p) {
   BfpTables& B = p->bfp;
-  cudaFree(B.up_off); cudaFree(B.up_npos); cudaFree(B.up_idx); cudaFree(B.dn_tab);
+  cudaFree(B.up_off); cudaFree(B.up_npos); cudaFree(B.up_idx); cudaFree(B.dn_tab); cudaFree(B.dn_btab2);
   cudaFree(B.e_up_int); cudaFree(B.e_dn_int); cudaFree(B.e_up_fx); cudaFree(B.e_dn_fx);
   B = BfpTables();
 }
@@ -601,12 +1175,93 @@ static BfpHubArgs bfp_args(const ed_plan_s* p) {
 }
 
 constexpr int MV_NT = 256;
+constexpr size_t MV_SMEM_LIMIT = 200 * 1024;
+
+static size_t v2_smem(const ed_plan_s* p) {
+  const size_t xstride = 2 * p->num_dn + 2;
+  return MV2_R * xstride * sizeof(int64_t) + (size_t)p->bfp.max_dn * (p->num_dn / 2) * sizeof(uint32_t);
+}
+
+static size_t v3_smem(const ed_plan_s* p) { return mv3_layout(p->num_dn, p->bfp.n_b2, p->bfp.max_up).total; }
+
+// block size of v3: warps take 64-column chunks; the fewest chunks per warp that fit in
+// MV3_MAXNT threads, then as few warps as carry them (3432 columns = 54 chunks -> 27 warps x 2)
+static int v3_threads(const ed_plan_s* p) {
+  const int64_t chunks = (p->num_dn + 63) / 64;
+  const int64_t per = (chunks + MV3_MAXNT / 32 - 1) / (MV3_MAXNT / 32);
+  const int64_t warps = (chunks + per - 1) / per;
+  return (int)std::min<int64_t>(MV3_MAXNT, 32 * std::max<int64_t>(1, warps));
+}
+
+// matvec variant: 3 (bulk-copied double-buffered rows, bond-major dn table) when both stages and
+// the table fit in shared memory, else 2 (resident slot table, one stage), else 1. Rows must
+// have an even length (16-byte row copies). CMPY_ED_MATVEC=1|2|3 forces a variant when possible.
+static int matvec_variant(const ed_plan_s* p) {
+  static int forced = -1;
+  if (forced < 0) {
+    const char* e = getenv("CMPY_ED_MATVEC");
+    forced = e ? atoi(e) : 0;
+  }
+  const size_t optin = (size_t)p->ctx->smem_optin;
+  const bool v2_ok = p->bfp.vec2 && v2_smem(p) + MV2_STATIC_SMEM <= optin && p->num_up >= 1;
+  // list entries are int32 element offsets u * nd: the vector must have fewer than 2^31 elements
+  const bool v3_ok = p->bfp.vec2 && p->bfp.dn_btab2 && v3_smem(p) + MV3_STATIC_SMEM <= optin && p->num_up >= 1 &&
+                     p->dim < ((int64_t)1 << 31);
+  if (forced == 1) return 1;
+  if (forced == 2) return v2_ok ? 2 : 1;
+  if (v3_ok) return 3;
+  return v2_ok ? 2 : 1;
+}
 
 static int bfp_matvec_grid(const ed_plan_s* p) {
+  if (matvec_variant(p) == 3)
+    return (int)std::min<int64_t>((p->num_up + MV3_R - 1) / MV3_R, (int64_t)p->ctx->num_sms);
+  if (matvec_variant(p) == 2)
+    return (int)std::min<int64_t>((p->num_up + MV2_R - 1) / MV2_R, (int64_t)p->ctx->num_sms);
   const size_t smem = (2 * p->num_dn + 1) * sizeof(int64_t);
-  int per_sm = (int)std::max<size_t>(1, (200 * 1024) / std::max<size_t>(smem, 1));
+  int per_sm = (int)std::max<size_t>(1, MV_SMEM_LIMIT / std::max<size_t>(smem, 1));
   per_sm = std::min(per_sm, 2048 / MV_NT);
   return (int)std::min<int64_t>(p->num_up, (int64_t)p->ctx->num_sms * per_sm);
+}
+
+template <bool DIAG64>
+static ed_status launch_v2(const ed_plan_s* p, int g, const int64_t* X, int64_t* W, double* partial,
+                           unsigned long long* partial_max, BfpState* st, cudaStream_t s) {
+  static std::atomic<uint64_t> done{0};
+  const uint64_t bit = 1ull << (p->device & 63);
+  if (!(done.load() & bit)) {
+    // the opt-in limit covers static + dynamic shared memory of the CTA
+    cudaFuncAttributes fa;
+    ED_CUDA(cudaFuncGetAttributes(&fa, k_bfp_hub_matvec2<DIAG64>));
+    if (fa.sharedSizeBytes > MV2_STATIC_SMEM) return fail(ED_ERR_CUDA, "k_bfp_hub_matvec2: static shared memory above its bound");
+    ED_CUDA(cudaFuncSetAttribute(k_bfp_hub_matvec2<DIAG64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 p->ctx->smem_optin - (int)fa.sharedSizeBytes));
+    done.fetch_or(bit);
+  }
+  k_bfp_hub_matvec2<DIAG64><<<g, MV2_NT, v2_smem(p), s>>>(bfp_args(p), X, W, partial, partial_max, st);
+  ED_CHECK_LAUNCH("k_bfp_hub_matvec2");
+  return ED_OK;
+}
+
+template <bool DIAG64>
+static ed_status launch_v3(const ed_plan_s* p, int g, const int64_t* X, int64_t* W, double* partial,
+                           unsigned long long* partial_max, BfpState* st, cudaStream_t s) {
+  static std::atomic<uint64_t> done{0};
+  const uint64_t bit = 1ull << (p->device & 63);
+  if (!(done.load() & bit)) {
+    cudaFuncAttributes fa;
+    ED_CUDA(cudaFuncGetAttributes(&fa, k_bfp_hub_matvec3<DIAG64>));
+    if (fa.sharedSizeBytes > MV3_STATIC_SMEM) return fail(ED_ERR_CUDA, "k_bfp_hub_matvec3: static shared memory above its bound");
+    ED_CUDA(cudaFuncSetAttribute(k_bfp_hub_matvec3<DIAG64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 p->ctx->smem_optin - (int)fa.sharedSizeBytes));
+    done.fetch_or(bit);
+  }
+  const BfpTables& B = p->bfp;
+  int* status = st ? &st->status : p->ctx->d_status;
+  k_bfp_hub_matvec3<DIAG64><<<g, v3_threads(p), v3_smem(p), s>>>(bfp_args(p), B.dn_btab2, B.n_b2, B.n_b2pos, B.max_up, X,
+                                                                 W, partial, partial_max, st, status);
+  ED_CHECK_LAUNCH("k_bfp_hub_matvec3");
+  return ED_OK;
 }
 
 // opt-in to large dynamic shared memory once per (kernel variant, device)
@@ -617,7 +1272,7 @@ static ed_status launch_variant(const ed_plan_s* p, size_t smem, int g, const in
   const uint64_t bit = 1ull << (p->device & 63);
   if (!(done.load() & bit)) {
     ED_CUDA(cudaFuncSetAttribute(k_bfp_hub_matvec<MV_NT, VEC2, DIAG64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 200 * 1024));
+                                 (int)MV_SMEM_LIMIT));
     done.fetch_or(bit);
   }
   k_bfp_hub_matvec<MV_NT, VEC2, DIAG64><<<g, MV_NT, smem, s>>>(bfp_args(p), X, W, partial, partial_max, st);
@@ -629,7 +1284,19 @@ static ed_status launch_bfp_matvec(const ed_plan_s* p, const int64_t* X, int64_t
                                    unsigned long long* partial_max, BfpState* st, cudaStream_t s) {
   const size_t smem = (2 * p->num_dn + 1) * sizeof(int64_t);
   const int g = bfp_matvec_grid(p);
-  const bool v2 = p->bfp.vec2 != 0, d64 = p->bfp.diag64 != 0;
+  const bool d64 = p->bfp.diag64 != 0;
+  // v2/v3 and the paired-column v1 move 16 bytes at a time (bulk row copies, v2 loads and
+  // stores): they need 16-byte aligned X and W, always true for the Lanczos store; other
+  // caller buffers take the one-column v1 kernel
+  const bool aligned = (((uintptr_t)X | (uintptr_t)W) & 15) == 0;
+  const int var = aligned ? matvec_variant(p) : 1;
+  if (var == 3)
+    return d64 ? launch_v3<true>(p, g, X, W, partial, partial_max, st, s)
+               : launch_v3<false>(p, g, X, W, partial, partial_max, st, s);
+  if (var == 2)
+    return d64 ? launch_v2<true>(p, g, X, W, partial, partial_max, st, s)
+               : launch_v2<false>(p, g, X, W, partial, partial_max, st, s);
+  const bool v2 = p->bfp.vec2 != 0 && aligned;
   if (v2 && !d64) return launch_variant<true, false>(p, smem, g, X, W, partial, partial_max, st, s);
   if (v2 && d64) return launch_variant<true, true>(p, smem, g, X, W, partial, partial_max, st, s);
   if (!v2 && !d64) return launch_variant<false, false>(p, smem, g, X, W, partial, partial_max, st, s);
@@ -648,7 +1315,7 @@ static BfpLayout bfp_layout(const ed_plan_s* p, int K, bool store) {
   BfpLayout L;
   const int64_t D = p->dim;
   L.nslots = store ? K + 1 : 3;
-  L.nparts = std::max(bfp_matvec_grid(p), p->ctx->num_sms * 4);
+  L.nparts = std::max(bfp_matvec_grid(p), p->ctx->num_sms * 8);
   size_t o = 0;
   L.off_R = o; o = al256(o + (size_t)L.nslots * D * 8);
   L.off_W = o; o = al256(o + (size_t)D * 8);
@@ -743,12 +1410,24 @@ static ed_status bfp_start(const ed_plan_s* p, BfpRun& r, const double* v0, doub
   return ED_OK;
 }
 
+// the update kernel of step k; the caller checks and counts the launch
+static ed_status launch_update(const ed_plan_s* p, BfpRun& r, int k, double* alpha, double* beta, cudaStream_t s) {
+  const bool vec = (p->dim % 2 == 0) && (((uintptr_t)r.v.R | (uintptr_t)r.W) & 15) == 0;
+  // one wave: four 256-thread blocks per SM (64 registers), two element pairs per thread in flight
+  const int g = std::min(r.L.nparts, p->ctx->num_sms * 4);
+  if (vec)
+    k_bfp_update<true><<<g, BT, 0, s>>>(r.v, k, r.W, r.part, r.partmax, beta, alpha, r.st, 0);
+  else
+    k_bfp_update<false><<<r.L.nparts, BT, 0, s>>>(r.v, k, r.W, r.part, r.partmax, beta, alpha, r.st, 0);
+  return ED_OK;
+}
+
 // one Lanczos step k: matvec + scalars + update (3 launches)
 static ed_status bfp_step(const ed_plan_s* p, BfpRun& r, int k, double* alpha, double* beta, cudaStream_t s) {
   const int gmv = bfp_matvec_grid(p);
   ED_TRY(launch_bfp_matvec(p, r.v.vec(k), r.W, r.part, r.partmax, r.st, s));
   k_bfp_scalars<<<1, BT, 0, s>>>(r.v, k, p->bfp.F, p->bfp.m_in, r.part, r.partmax, gmv, alpha, beta, r.st);
-  k_bfp_update<<<r.L.nparts, BT, 0, s>>>(r.v, k, r.W, r.part, r.partmax, beta, alpha, r.st, 0);
+  ED_TRY(launch_update(p, r, k, alpha, beta, s));
   ED_CHECK_LAUNCH_N("bfp step", 2);
   return ED_OK;
 }
@@ -783,7 +1462,7 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
     if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k + 1], s));
     k_bfp_scalars<<<1, BT, 0, s>>>(r.v, k, p->bfp.F, p->bfp.m_in, r.part, r.partmax, bfp_matvec_grid(p), alpha,
                                    beta, r.st);
-    k_bfp_update<<<r.L.nparts, BT, 0, s>>>(r.v, k, r.W, r.part, r.partmax, beta, alpha, r.st, 0);
+    ED_TRY(launch_update(p, r, k, alpha, beta, s));
     uint64_t nl = 2;
     if (prm->check_every > 0 && ((k + 1) % prm->check_every == 0) && k + 1 < Km) {
       k_lz_check_bfp<<<1, 256, 0, s>>>(alpha, beta, k, prm->tol, r.st, r.c, r.work);
@@ -806,6 +1485,7 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
   res->steps = hs.steps;
   res->converged = hs.stop;
   res->status = hs.status;
+  if (hs.status == DEV_TIMEOUT) return fail(ED_ERR_TIMEOUT, "fixed-point matvec: a bounded wait for a row copy ran out");
   res->matvec_ms = 0.0;
   res->matvecs = 0;
   if (prm->profile) {
@@ -850,6 +1530,7 @@ ed_status bfp_lanczos_coeffs(const ed_plan_s* p, int K, const double* start, voi
   ED_CUDA(cudaMemcpyAsync(&hs, r.st, sizeof(BfpState), cudaMemcpyDeviceToHost, s));
   ED_CUDA(cudaMemcpyAsync(&b0, beta, sizeof(double), cudaMemcpyDeviceToHost, s));
   ED_CUDA(cudaStreamSynchronize(s));
+  if (hs.status == DEV_TIMEOUT) return fail(ED_ERR_TIMEOUT, "fixed-point matvec: a bounded wait for a row copy ran out");
   *steps = hs.stop ? hs.steps : Km;
   *norm = b0;
   // the continued fraction expects beta[0] = 0 and beta[k] the couplings

@@ -9,6 +9,7 @@
 #include "../../include/cmpy_ed.h"
 
 #define ED_MAX_SITES 62
+#define ED_MAX_BONDS 128
 
 namespace ed {
 
@@ -47,6 +48,7 @@ inline cudaStream_t as_stream(ed_stream_t s) { return reinterpret_cast<cudaStrea
 struct DeviceContext {
   int device = -1;
   int num_sms = 0;
+  int smem_optin = 0;  // largest shared memory (static + dynamic) one CTA may opt in to
   uint64_t* d_binom = nullptr;
   int* d_status = nullptr;  // device status word (first error code a kernel records)
 };

@@ -22,7 +22,6 @@ struct BondList {
   int s2[128];
   double hop[128];
 };
-#define ED_MAX_BONDS 128
 
 __global__ void k_state_energy(const uint64_t* __restrict__ states, int64_t n, FermionParams fp,
                                const double* __restrict__ eps, double* __restrict__ out) {
