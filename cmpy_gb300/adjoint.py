@@ -87,7 +87,12 @@ def lanczos_taped(plan: E.Plan, start: torch.Tensor, m: int, c: int = 16, breakd
                   tol: float = 0.0, check_every: int = 10) -> LanczosTape:
     """Plain Lanczos from `start` keeping (alpha, beta) and checkpoints every c steps. With
     tol > 0 it stops once the lowest Ritz pair has residual <= tol * max(1, |E|) (before
-    ghost copies of the converged value appear in T)."""
+    ghost copies of the converged value appear in T).
+
+    The recurrence runs in blocks of `check_every` steps without host synchronisation; the
+    breakdown test (beta_{k+1} <= breakdown * (|alpha_k| + beta_k)) and the convergence test
+    read the block's scalars once. Steps computed after a breakdown inside a block are
+    discarded, so the tape is the same as with a per-step test."""
     s = start.reshape(-1)
     b0 = torch.linalg.norm(s)
     q = s / b0
@@ -95,26 +100,38 @@ def lanczos_taped(plan: E.Plan, start: torch.Tensor, m: int, c: int = 16, breakd
     alpha, beta = [], [b0]
     ckpt = {}
     m = int(min(m, plan.dim))
-    for k in range(m):
-        if k % c == 0:
-            ckpt[k] = (qp, q)
-        w = plan.matvec(q)
-        a = torch.dot(q, w)
-        r = w - a * q
-        if qp is not None:
-            r = r - beta[k] * qp
-        bn = torch.linalg.norm(r)
-        alpha.append(a)
-        beta.append(bn)
-        scale = abs(a.item()) + (beta[k].item() if k > 0 else 0.0)
-        if not bn.item() > breakdown * scale:
-            break
-        if tol > 0 and (k + 1) % check_every == 0:
+    blk = max(1, int(check_every))
+    stop = None
+    k = 0
+    while k < m and stop is None:
+        k_end = min(m, k + blk)
+        for kk in range(k, k_end):
+            if kk % c == 0:
+                ckpt[kk] = (qp, q)
+            w = plan.matvec(q)
+            a = torch.dot(q, w)
+            r = w - a * q
+            if qp is not None:
+                r = r - beta[kk] * qp
+            bn = torch.linalg.norm(r)
+            alpha.append(a)
+            beta.append(bn)
+            qp, q = q, r / bn  # inf/nan after an exact breakdown: those steps are dropped below
+        a_h = torch.stack(alpha[k:k_end]).cpu().numpy()
+        b_h = torch.stack(beta[k:k_end + 1]).cpu().numpy()
+        for j in range(k, k_end):
+            scale = abs(a_h[j - k]) + (b_h[j - k] if j > 0 else 0.0)
+            if not b_h[j - k + 1] > breakdown * scale:
+                stop = j + 1
+                break
+        if stop is None and tol > 0 and k_end % blk == 0:
             res, e = _lowest_ritz_residual(alpha, beta)
             if res <= tol * max(1.0, abs(e)):
-                break
-        qp, q = q, r / bn
-    return LanczosTape(torch.stack(alpha), torch.stack(beta), ckpt, c, len(alpha))
+                stop = k_end
+        k = k_end
+    mm = stop if stop is not None else len(alpha)
+    ckpt = {kk: v for kk, v in ckpt.items() if kk < mm}
+    return LanczosTape(torch.stack(alpha[:mm]), torch.stack(beta[:mm + 1]), ckpt, c, mm)
 
 
 def _segment(plan, tape: LanczosTape, k0: int, k1: int):

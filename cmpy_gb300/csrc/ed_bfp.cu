@@ -577,10 +577,13 @@ __device__ __forceinline__ int64_t shfl64(int64_t v, int src) {
   return (int64_t)__shfl_sync(0xffffffffu, (long long)v, src);
 }
 
-template <bool DIAG64>
+// UPW: the up-neighbour sums were written into W by k_bfp_up_panels (two-pass H·v); the kernel
+// reads them instead of gathering and overwrites W with the result (each element read, then
+// written, by the same thread)
+template <bool DIAG64, bool UPW>
 __global__ void __launch_bounds__(MV3_MAXNT, 1)
     k_bfp_hub_matvec3(BfpHubArgs a, const uint32_t* __restrict__ btab2, int n_b2, int n_b2pos, int max_up,
-                      const int64_t* __restrict__ X, int64_t* __restrict__ W, double* partial,
+                      const int64_t* __restrict__ X, int64_t* W, double* partial,
                       unsigned long long* partial_max, BfpState* st, int* status) {
   if (st && *(volatile int*)&st->stop) return;
   extern __shared__ __align__(128) unsigned char sm3[];
@@ -604,7 +607,7 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
   auto stage = [&](int64_t g, int s) {
     const int64_t u0 = g * MV3_R;
     const int nr = (int)min((int64_t)MV3_R, nu - u0);
-    for (int t = tid; t < MV3_R * L.lstride; t += nt) {
+    for (int t = tid; t < (UPW ? 0 : MV3_R * L.lstride); t += nt) {
       const int r = t / L.lstride, e = t - r * L.lstride;
       if (r >= nr) continue;
       const int64_t u = u0 + r;
@@ -683,9 +686,9 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
     }
     const int32_t* l0 = lst + (s * MV3_R + 0) * L.lstride;
     const int32_t* l1 = lst + (s * MV3_R + 1) * L.lstride;
-    const int32_t cp0 = cnt[(s * MV3_R + 0) * 4 + 0], cn0 = cnt[(s * MV3_R + 0) * 4 + 1];
-    const int32_t cp1 = cnt[(s * MV3_R + 1) * 4 + 0], cn1 = cnt[(s * MV3_R + 1) * 4 + 1];
-    const int64_t corr0 = cnt[(s * MV3_R + 0) * 4 + 2], corr1 = cnt[(s * MV3_R + 1) * 4 + 2];
+    const int32_t cp0 = UPW ? 0 : cnt[(s * MV3_R + 0) * 4 + 0], cn0 = UPW ? 0 : cnt[(s * MV3_R + 0) * 4 + 1];
+    const int32_t cp1 = UPW ? 0 : cnt[(s * MV3_R + 1) * 4 + 0], cn1 = UPW ? 0 : cnt[(s * MV3_R + 1) * 4 + 1];
+    const int64_t corr0 = UPW ? 0 : cnt[(s * MV3_R + 0) * 4 + 2], corr1 = UPW ? 0 : cnt[(s * MV3_R + 1) * 4 + 2];
     const uint64_t su0 = __ldg(a.up_states + row0), su1 = __ldg(a.up_states + row0 + (nr > 1 ? 1 : 0));
     const int64_t eu0 = DIAG64 ? 0 : (int64_t)__ldg(a.e_up + row0);
     const int64_t eu1 = DIAG64 ? 0 : (int64_t)__ldg(a.e_up + row0 + (nr > 1 ? 1 : 0));
@@ -700,6 +703,14 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
       const uint64_t sd_lo = __ldg(a.dn_states + c_lo), sd_hi = __ldg(a.dn_states + c_hi);
       const int32_t e32_lo = DIAG64 ? 0 : __ldg(a.e_dn + c_lo), e32_hi = DIAG64 ? 0 : __ldg(a.e_dn + c_hi);
       const int64_t e64_lo = DIAG64 ? __ldg(a.e_dn_fx + c_lo) : 0, e64_hi = DIAG64 ? __ldg(a.e_dn_fx + c_hi) : 0;
+      int64_t up_lo[2], up_hi[2];
+      if (UPW) {
+        // the up-neighbour sums of the two rows, written by the panel pass
+        up_lo[0] = W[row0 * nd + c_lo];
+        up_hi[0] = W[row0 * nd + c_hi];
+        up_lo[1] = nr > 1 ? W[(row0 + 1) * nd + c_lo] : 0;
+        up_hi[1] = nr > 1 ? W[(row0 + 1) * nd + c_hi] : 0;
+      } else {
       // up neighbours in pair layout: lane l loads columns base + 2l, base + 2l + 1 (16 bytes)
       const int64_t cpair = base + 2 * lane;
       const int64_t* xc = X + min(cpair, nd - 2);  // out-of-range lanes load a valid pair, unused
@@ -717,7 +728,6 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
       // to the lane-contiguous layout: column base + l sits in lane l/2 (element l&1),
       // column base + 32 + l in lane 16 + l/2
       const bool odd = lane & 1;
-      int64_t up_lo[2], up_hi[2];
       {
         const int s_lo = lane >> 1, s_hi = 16 + (lane >> 1);
         const int64_t a0 = shfl64(u0.x, s_lo), b0 = shfl64(u0.y, s_lo), a1 = shfl64(u1.x, s_lo), b1 = shfl64(u1.y, s_lo);
@@ -726,6 +736,7 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
         up_lo[1] = odd ? b1 : a1;
         up_hi[0] = odd ? d0 : c0;
         up_hi[1] = odd ? d1 : c1;
+      }
       }
 #pragma unroll
       for (int half = 0; half < 2; ++half) {
@@ -783,6 +794,65 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
   if (tid == 0) {
     partial[blockIdx.x] = sdot;
     partial_max[blockIdx.x] = m;
+  }
+}
+
+// ---- two-pass H·v, pass 1: up-neighbour sums by column panels ---------------------------------
+// The up-hop part of H·v, W[u, c] = sum_{u'} (+-) X[u', c], is a sparse-times-dense product. A
+// CTA loads a panel of MV_PW = 4 columns of ALL rows (nu x 32 bytes) into shared memory once and
+// forms the sums of every row from there, so each element of X crosses from L2 once instead of
+// once per up-neighbour (7.5 times at 14 sites). Two CTAs per SM: one loads while the other sums.
+// The dn/diagonal pass (k_bfp_hub_matvec3<., true>) then finishes W in place.
+constexpr int MV_PW = 4;
+constexpr int UP_NT = 512;
+
+__global__ void __launch_bounds__(UP_NT, 2)
+    k_bfp_up_panels(const int32_t* __restrict__ up_off, const int32_t* __restrict__ up_npos,
+                    const int32_t* __restrict__ up_idx, int64_t nu, int64_t nd, const int64_t* __restrict__ X,
+                    int64_t* __restrict__ W, const BfpState* st) {
+  if (st && *(const volatile int*)&st->stop) return;
+  extern __shared__ __align__(16) longlong2 pan[];  // [nu][2]: columns c0..c0+3 of every row
+  const int64_t npan = nd / MV_PW;
+  for (int64_t pnl = blockIdx.x; pnl < npan; pnl += gridDim.x) {
+    const int64_t c0 = pnl * MV_PW;
+    // load the panel: two 16-byte loads per row, four rows per thread in flight
+    for (int64_t u = threadIdx.x; u < nu; u += 4 * UP_NT) {
+      longlong2 v[8];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int64_t uu = min(u + q * UP_NT, nu - 1);
+        const longlong2* src = (const longlong2*)(X + uu * nd + c0);
+        v[2 * q] = __ldg(src);
+        v[2 * q + 1] = __ldg(src + 1);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int64_t uu = u + q * UP_NT;
+        if (uu < nu) {
+          pan[2 * uu] = v[2 * q];
+          pan[2 * uu + 1] = v[2 * q + 1];
+        }
+      }
+    }
+    __syncthreads();
+    for (int64_t u = threadIdx.x; u < nu; u += UP_NT) {
+      const int32_t o0 = __ldg(up_off + u), o1 = __ldg(up_off + u + 1), op = o0 + __ldg(up_npos + u);
+      longlong2 a = make_longlong2(0, 0), b = make_longlong2(0, 0);
+      for (int32_t e = o0; e < op; ++e) {
+        const int32_t n = __ldg(up_idx + e);
+        const longlong2 x0 = pan[2 * n], x1 = pan[2 * n + 1];
+        a.x += x0.x; a.y += x0.y; b.x += x1.x; b.y += x1.y;
+      }
+      for (int32_t e = op; e < o1; ++e) {
+        const int32_t n = __ldg(up_idx + e);
+        const longlong2 x0 = pan[2 * n], x1 = pan[2 * n + 1];
+        a.x -= x0.x; a.y -= x0.y; b.x -= x1.x; b.y -= x1.y;
+      }
+      longlong2* dst = (longlong2*)(W + u * nd + c0);
+      dst[0] = a;
+      dst[1] = b;
+    }
+    __syncthreads();  // the panel buffer is reloaded next
   }
 }
 
@@ -1207,14 +1277,17 @@ static int matvec_variant(const ed_plan_s* p) {
   // list entries are int32 element offsets u * nd: the vector must have fewer than 2^31 elements
   const bool v3_ok = p->bfp.vec2 && p->bfp.dn_btab2 && v3_smem(p) + MV3_STATIC_SMEM <= optin && p->num_up >= 1 &&
                      p->dim < ((int64_t)1 << 31);
+  // two-pass (4): column panels of 4 (nd % 4 == 0), a panel of all rows in half the shared memory
+  const bool v4_ok = v3_ok && p->num_dn % MV_PW == 0 && (size_t)p->num_up * MV_PW * 8 + 1024 <= optin / 2;
   if (forced == 1) return 1;
   if (forced == 2) return v2_ok ? 2 : 1;
+  if (forced == 4 && v4_ok) return 4;  // measured slower than 3 on GB300 (kept for comparison)
   if (v3_ok) return 3;
   return v2_ok ? 2 : 1;
 }
 
 static int bfp_matvec_grid(const ed_plan_s* p) {
-  if (matvec_variant(p) == 3)
+  if (matvec_variant(p) >= 3)
     return (int)std::min<int64_t>((p->num_up + MV3_R - 1) / MV3_R, (int64_t)p->ctx->num_sms);
   if (matvec_variant(p) == 2)
     return (int)std::min<int64_t>((p->num_up + MV2_R - 1) / MV2_R, (int64_t)p->ctx->num_sms);
@@ -1243,23 +1316,32 @@ static ed_status launch_v2(const ed_plan_s* p, int g, const int64_t* X, int64_t*
   return ED_OK;
 }
 
-template <bool DIAG64>
+template <bool DIAG64, bool UPW>
 static ed_status launch_v3(const ed_plan_s* p, int g, const int64_t* X, int64_t* W, double* partial,
                            unsigned long long* partial_max, BfpState* st, cudaStream_t s) {
   static std::atomic<uint64_t> done{0};
   const uint64_t bit = 1ull << (p->device & 63);
   if (!(done.load() & bit)) {
     cudaFuncAttributes fa;
-    ED_CUDA(cudaFuncGetAttributes(&fa, k_bfp_hub_matvec3<DIAG64>));
+    ED_CUDA(cudaFuncGetAttributes(&fa, k_bfp_hub_matvec3<DIAG64, UPW>));
     if (fa.sharedSizeBytes > MV3_STATIC_SMEM) return fail(ED_ERR_CUDA, "k_bfp_hub_matvec3: static shared memory above its bound");
-    ED_CUDA(cudaFuncSetAttribute(k_bfp_hub_matvec3<DIAG64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    ED_CUDA(cudaFuncSetAttribute(k_bfp_hub_matvec3<DIAG64, UPW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  p->ctx->smem_optin - (int)fa.sharedSizeBytes));
+    if (UPW) ED_CUDA(cudaFuncSetAttribute(k_bfp_up_panels, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          p->ctx->smem_optin / 2));
     done.fetch_or(bit);
   }
   const BfpTables& B = p->bfp;
   int* status = st ? &st->status : p->ctx->d_status;
-  k_bfp_hub_matvec3<DIAG64><<<g, v3_threads(p), v3_smem(p), s>>>(bfp_args(p), B.dn_btab2, B.n_b2, B.n_b2pos, B.max_up, X,
-                                                                 W, partial, partial_max, st, status);
+  if (UPW) {
+    const size_t psm = (size_t)p->num_up * MV_PW * 8;
+    const int gp = (int)std::min<int64_t>(p->num_dn / MV_PW, (int64_t)p->ctx->num_sms * 2);
+    k_bfp_up_panels<<<gp, UP_NT, psm, s>>>(B.up_off, B.up_npos, B.up_idx, p->num_up, p->num_dn, X, W, st);
+    ED_CHECK_LAUNCH("k_bfp_up_panels");
+  }
+  k_bfp_hub_matvec3<DIAG64, UPW><<<g, v3_threads(p), v3_smem(p), s>>>(bfp_args(p), B.dn_btab2, B.n_b2, B.n_b2pos,
+                                                                      B.max_up, X, W, partial, partial_max, st,
+                                                                      status);
   ED_CHECK_LAUNCH("k_bfp_hub_matvec3");
   return ED_OK;
 }
@@ -1290,9 +1372,12 @@ static ed_status launch_bfp_matvec(const ed_plan_s* p, const int64_t* X, int64_t
   // caller buffers take the one-column v1 kernel
   const bool aligned = (((uintptr_t)X | (uintptr_t)W) & 15) == 0;
   const int var = aligned ? matvec_variant(p) : 1;
+  if (var == 4)
+    return d64 ? launch_v3<true, true>(p, g, X, W, partial, partial_max, st, s)
+               : launch_v3<false, true>(p, g, X, W, partial, partial_max, st, s);
   if (var == 3)
-    return d64 ? launch_v3<true>(p, g, X, W, partial, partial_max, st, s)
-               : launch_v3<false>(p, g, X, W, partial, partial_max, st, s);
+    return d64 ? launch_v3<true, false>(p, g, X, W, partial, partial_max, st, s)
+               : launch_v3<false, false>(p, g, X, W, partial, partial_max, st, s);
   if (var == 2)
     return d64 ? launch_v2<true>(p, g, X, W, partial, partial_max, st, s)
                : launch_v2<false>(p, g, X, W, partial, partial_max, st, s);
