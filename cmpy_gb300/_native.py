@@ -161,6 +161,8 @@ _SIGNATURES = {
     "ed_matvec_fixed": (I32, [PLAN, P, C.c_int32, P, C.POINTER(C.c_int32), C.POINTER(I32), P]),
     "ed_gf_continued_fraction": (I32, [P, P, I32, F64, F64, I32, P, I64, P, I32, P]),
     "ed_lehmann_accumulate": (I32, [P, I64, P, I64, P, F64, F64, P, I64, P, P]),
+    "ed_tevo_sum": (I32, [P, P, I64, F64, I32, P, I64, P, I32, P]),
+    "ed_laplace_t2z": (I32, [P, P, I64, P, I64, I32, P, P]),
 }
 
 

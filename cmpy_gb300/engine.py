@@ -459,6 +459,35 @@ def continued_fraction(alpha, beta, norm2: float, z, e0: float = 0.0, sign: int 
     return g
 
 
+def tevo_sum(lam, w, e0: float, sign: int, times, out: torch.Tensor | None = None) -> torch.Tensor:
+    """-i*sign * sum_k w_k exp(-i sign (lam_k - e0) t) for every t (complex128 on device)."""
+    la = _as_dev_f64(lam).reshape(-1)
+    wt = _as_dev_f64(w).reshape(-1)
+    tt = _as_dev_f64(times).reshape(-1)
+    if la.numel() != wt.numel():
+        raise ValueError("lam and w must have the same length")
+    acc = out is not None
+    g = out if acc else torch.empty(tt.numel(), dtype=torch.complex128, device=device())
+    N.check(N.lib().ed_tevo_sum(N.ptr(la), N.ptr(wt), la.numel(), float(e0), int(sign), N.ptr(tt), tt.numel(),
+                                N.ptr(torch.view_as_real(g)), int(acc), _stream()))
+    return g
+
+
+def laplace_t2z(times, gf_t, z, method: str = "lin") -> torch.Tensor:
+    """int_{t_0}^{t_last} e^{izt} g(t) dt of samples g(t_j) (piecewise-linear "lin" or "trapz")."""
+    tt = _as_dev_f64(times).reshape(-1)
+    gt = _as_dev_c128(gf_t).reshape(-1)
+    zt = _as_dev_c128(z).reshape(-1)
+    if tt.numel() != gt.numel():
+        raise ValueError("times and gf_t must have the same length")
+    m = {"lin": 0, "trapz": 1}[method]
+    out = torch.empty_like(zt)
+    N.check(N.lib().ed_laplace_t2z(N.ptr(tt), N.ptr(torch.view_as_real(gt)), tt.numel(),
+                                   N.ptr(torch.view_as_real(zt)), zt.numel(), m, N.ptr(torch.view_as_real(out)),
+                                   _stream()))
+    return out
+
+
 def lehmann_accumulate(evals, evals_p1, overlap, beta: float, emin: float, z, g: torch.Tensor) -> torch.Tensor:
     e = _as_dev_f64(evals)
     ep = _as_dev_f64(evals_p1)

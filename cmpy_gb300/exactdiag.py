@@ -37,6 +37,12 @@ __all__ = [
     "gf_lehmann",
     "gf_lehmann_zero_temperature",
     "gf_continued_fraction",
+    "greens_lehmann",
+    "gf_lehmann_offdiag",
+    "gf_greater",
+    "gf_lesser",
+    "gf_tevo",
+    "fourier_t2z",
     "iter_lanczos_coeffs",
     "lanczos_coeffs",
     "lanczos_matrix",
@@ -237,6 +243,63 @@ def gf_lehmann(model, z, beta, pos=0, sigma=UP, eig_cache=None, occ=True, jw_sig
     return data
 
 
+def _lehmann_pair(model, z, beta, i, j, sigma, eig_cache, jw_sign):
+    """Running Lehmann accumulation over all sectors with an upper sector (the structure of
+    lehmann_full.py:48-97 and exactdiag.py:215-245) with the overlap <n|c_i|m><m|c^dag_j|n>;
+    returns (gf, part), part being the partition function relative to the running E0."""
+    from .operators import CreationOperator
+
+    basis = model.basis
+    eig_cache = eig_cache if eig_cache is not None else dict()
+    zt = E._as_dev_c128(z)
+    gf = torch.zeros_like(zt)
+    part = 0.0
+    e0 = np.inf
+    for n_up, n_dn in basis.iter_fillings():
+        sector = model.get_sector(n_up, n_dn)
+        sector_p1 = basis.upper_sector(n_up, n_dn, sigma)
+        if sector_p1 is None:
+            continue
+        w, v = _solve_sector_dev(model, sector, eig_cache)
+        wp, vp = _solve_sector_dev(model, sector_p1, eig_cache)
+        w_t = E._as_dev_f64(w)
+        min_energy = float(w_t.min().item())
+        factor = 1.0
+        if min_energy < e0:
+            factor = float(np.exp(-beta * (e0 - min_energy)))
+            e0 = min_energy
+        part = part * factor + float(torch.exp(-beta * (w_t - e0)).sum().item())
+        if factor != 1.0:
+            gf *= factor
+        V = E._as_dev_f64(v)
+        Vp = E._as_dev_f64(vp)
+        a_i = Vp.t() @ CreationOperator(sector, sector_p1, pos=i, sigma=sigma, jw_sign=jw_sign)._apply_dev(V)
+        if j == i:
+            ov = a_i**2
+        else:
+            a_j = Vp.t() @ CreationOperator(sector, sector_p1, pos=j, sigma=sigma, jw_sign=jw_sign)._apply_dev(V)
+            ov = a_i * a_j  # <n|c_i|m><m|c^dag_j|n> (real eigenvectors)
+        E.lehmann_accumulate(w_t, wp, ov, float(beta), e0, zt, gf)
+    return gf, part
+
+
+def greens_lehmann(model, z, beta, i, j, sigma=UP, occ=True, eig_cache=None, jw_sign: bool = False):
+    """Lehmann sum of the reference's G_ij draft (lehmann_full.py:48-97), completed: the
+    overlap is <n|c_i|m><m|c^dag_j|n>, and like the draft the sum is returned without dividing
+    by the partition function. The draft itself computes neither G_ij nor G_ii: its sector loop
+    variable shadows `i` (the operator acts on site = sector index) and the c^dag_j factor is
+    commented out (lehmann_full.py:19-25, 63-90)."""
+    gf, _ = _lehmann_pair(model, z, beta, i, j, sigma, eig_cache, jw_sign)
+    return gf.cpu().numpy()
+
+
+def gf_lehmann_offdiag(model, z, beta, i, j, sigma=UP, eig_cache=None, jw_sign: bool = False):
+    """Thermal G_ij(z) = Z^-1 sum_{n,m} <n|c_i|m><m|c^dag_j|n> (e^{-beta E_n} + e^{-beta E_m}) /
+    (z - E_m + E_n) over all sectors; i = j gives gf_lehmann(pos=i)."""
+    gf, part = _lehmann_pair(model, z, beta, i, j, sigma, eig_cache, jw_sign)
+    return (gf / part).cpu().numpy()
+
+
 def _neighbour(model, n_up, n_dn, sigma, delta):
     nu, nd = (n_up + delta, n_dn) if sigma == UP else (n_up, n_dn + delta)
     if not (0 <= nu <= model.num_sites and 0 <= nd <= model.num_sites):
@@ -291,6 +354,81 @@ def gf_continued_fraction(model, z, n_up: int, n_dn: int, gs_energy: float, gs_s
         E.continued_fraction(a, b, nrm * nrm, zt, e0=gs_energy, sign=sign, out=g)
     out = g.cpu().numpy()
     return (out, coeffs) if return_coeffs else out
+
+
+# -- real-time Green's functions (cmpy/exactdiag.py:248-316) -------------------------------
+
+
+def _tevo_part(model, gs, times: np.ndarray, pos: int, sigma: int, delta: int, n_lev: Optional[int],
+               jw_sign: bool) -> Optional[torch.Tensor]:
+    """-i e^{iE0 t}<gs|c e^{-iHt} c^dag|gs> (delta=+1) or +i e^{-iE0 t}<gs|c^dag e^{iHt} c|gs>
+    (delta=-1) on the device. The reference propagates with scipy expm_multiply; here the
+    Lanczos tridiagonal T_m of the start vector gives <phi|e^{-iHt}|phi> = |phi|^2 e1^T
+    e^{-iT_m t} e1, i.e. a sum over the eigenpairs of T_m (exact once m reaches the dimension,
+    and converged long before that for ||H|| t << m)."""
+    nb = _neighbour(model, gs.n_up, gs.n_dn, sigma, delta)
+    if nb is None:
+        return None
+    plan = _sector_plan(model, gs.n_up, gs.n_dn)
+    tplan = _sector_plan(model, *nb)
+    psi = E._as_dev_f64(gs.state).reshape(-1)
+    phi = plan.apply_fermion(tplan, pos, sigma, delta > 0, psi, jw_sign=jw_sign)
+    steps = tplan.dim if n_lev is None else min(int(n_lev), tplan.dim)
+    a, b, nrm = E.lanczos_coeffs(tplan, phi, max_steps=steps)
+    m = a.numel()
+    tt = E._as_dev_f64(times)
+    if m == 0 or nrm == 0.0:
+        return torch.zeros(tt.numel(), dtype=torch.complex128, device=E.device())
+    T = torch.diag(a)
+    if m > 1:
+        T = T + torch.diag(b[1:m], 1) + torch.diag(b[1:m], -1)
+    lam, U = torch.linalg.eigh(T)
+    w = (nrm * nrm) * U[0, :] ** 2
+    return E.tevo_sum(lam, w, float(gs.energy), 1 if delta > 0 else -1, tt)
+
+
+def _tevo(model, gs, start, stop, num, pos, sigma, delta, n_lev, jw_sign):
+    times = np.linspace(start, stop, num)
+    g = _tevo_part(model, gs, times, pos, sigma, delta, n_lev, jw_sign)
+    if g is None:
+        logger.warning("%s sector not found!", "Upper" if delta > 0 else "Lower")
+        return times, np.zeros_like(times)
+    return times, g.cpu().numpy()
+
+
+def gf_greater(model, gs, start, stop, num=1000, pos=0, sigma=UP, n_lev: Optional[int] = 2000,
+               jw_sign: bool = False):
+    """Greater Green's function -i e^{i E0 t} <gs|c e^{-iHt} c^dag|gs> at `num` times in
+    [start, stop] (cmpy/exactdiag.py:248-273). n_lev caps the Krylov dimension (None: the
+    sector dimension)."""
+    return _tevo(model, gs, start, stop, num, pos, sigma, +1, n_lev, jw_sign)
+
+
+def gf_lesser(model, gs, start, stop, num=1000, pos=0, sigma=UP, n_lev: Optional[int] = 2000,
+              jw_sign: bool = False):
+    """Lesser Green's function +i e^{-i E0 t} <gs|c^dag e^{iHt} c|gs> (cmpy/exactdiag.py:276-301)."""
+    return _tevo(model, gs, start, stop, num, pos, sigma, -1, n_lev, jw_sign)
+
+
+def gf_tevo(model, start, stop, num=1000, pos=0, sigma=UP, n_lev: Optional[int] = 2000):
+    """G(t) = G^>(t) - G^<(t) of the ground state (cmpy/exactdiag.py:304-308)."""
+    gs = compute_groundstate(model)
+    times, gg = gf_greater(model, gs, start, stop, num, pos, sigma, n_lev)
+    _, gl = gf_lesser(model, gs, start, stop, num, pos, sigma, n_lev)
+    return times, gg - gl
+
+
+def fourier_t2z(times, gf_t, omegas, delta=1e-2, eta=None, method: str = "lin"):
+    """G(z) = int e^{izt} G(t) dt at z = omega + i eta, eta = -ln(delta)/t_last by default
+    (cmpy/exactdiag.py:311-316). The reference calls gftool.fourier.tt2z; its default rule,
+    the exact integral of the piecewise-linear interpolant of G(t), is evaluated on the device
+    ("trapz" selects the trapezoidal rule)."""
+    times = np.asarray(times, dtype=np.float64)
+    if eta is None:
+        eta = -np.log(delta) / times[-1]
+    z = np.asarray(omegas) + 1j * eta
+    gw = E.laplace_t2z(times, gf_t, z, method=method)
+    return z, gw.cpu().numpy()
 
 
 # -- Lanczos helpers (cmpy/exactdiag.py:324-375) on the device ------------------------------

@@ -368,6 +368,25 @@ ED_API ed_status ed_lehmann_accumulate(const double* d_evals, int64_t n_d,
                                        const double* d_z, int64_t n_z, double* d_g,
                                        ed_stream_t stream);
 
+/* Real-time Green's function from Krylov spectral data: with (lam_k, w_k) the eigenvalues of
+ * the Lanczos tridiagonal of c^dag|gs> (resp. c|gs>) and w_k = norm^2 * U_0k^2 their weights,
+ *   out[n] (+)= -i*sign * sum_k w_k exp(-i sign (lam_k - e0) t_n)
+ * over n_t times (interleaved complex FP64 out). sign = +1 gives the greater function
+ * -i e^{i E0 t} <gs|c e^{-iHt} c^dag|gs> of gf_greater (cmpy/exactdiag.py:248-273), sign = -1
+ * the lesser function +i e^{-i E0 t} <gs|c^dag e^{iHt} c|gs> of gf_lesser (exactdiag.py:276-301),
+ * which the reference evaluates with scipy expm_multiply. */
+ED_API ed_status ed_tevo_sum(const double* d_lam, const double* d_w, int64_t m, double e0, int sign,
+                             const double* d_t, int64_t n_t, double* d_out, int accumulate,
+                             ed_stream_t stream);
+
+/* Laplace transform G(z) = int_{t_0}^{t_last} e^{i z t} g(t) dt of complex samples g(t_j) to n_z
+ * complex frequencies — fourier_t2z (cmpy/exactdiag.py:311-316), which calls
+ * gftool.fourier.tt2z. method 0: exact integral of the piecewise-linear interpolant of g
+ * (gftool's default rule, tt2z_lin); method 1: trapezoidal rule (tt2z_trapz). */
+ED_API ed_status ed_laplace_t2z(const double* d_t, const double* d_gt, int64_t n_t,
+                                const double* d_z, int64_t n_z, int method, double* d_out,
+                                ed_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

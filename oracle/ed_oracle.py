@@ -420,3 +420,135 @@ def tridiag_lowest(a, b):
     w = la.eigh_tridiagonal(np.asarray(a), np.asarray(b[1: len(a)]), eigvals_only=True, select="i",
                             select_range=(0, 0))
     return float(w[0])
+
+
+# ---- real-time Green's functions: cmpy/exactdiag.py:248-316 ---------------------------------
+
+
+def gf_time_dense(H_target: np.ndarray, start_vec: np.ndarray, e0: float, times, greater: bool) -> np.ndarray:
+    """gf_greater (exactdiag.py:248-273) / gf_lesser (exactdiag.py:276-301) from the dense
+    eigenpairs of the target sector: with phi = c^dag|gs> (greater) or c|gs> (lesser),
+      greater: -i e^{i E0 t} <phi|e^{-iHt}|phi>,   lesser: +i e^{-i E0 t} <phi|e^{+iHt}|phi>.
+    The reference evaluates e^{-+iHt} phi with scipy expm_multiply; the spectral sum is the
+    same function."""
+    w, V = np.linalg.eigh(H_target)
+    amp = (V.T @ np.asarray(start_vec, dtype=np.float64)) ** 2
+    t = np.asarray(times, dtype=np.float64)
+    s = 1.0 if greater else -1.0
+    phase = np.exp(-1j * s * np.outer(t, w - e0))
+    return -1j * s * (phase @ amp)
+
+
+def laplace_lin(times, gf_t, z) -> np.ndarray:
+    """int_{t_0}^{t_last} e^{izt} g(t) dt of the piecewise-linear interpolant of g — the rule
+    gftool.fourier.tt2z applies by default (tt2z_lin; gftool >= 0.10, pinned by cmpy's
+    setup.cfg:30 / requirements.txt:11, absent here): per segment h e^{u t_j} [g_j phi2(uh) +
+    g_{j+1} (phi1 - phi2)(uh)], u = iz, phi1(x) = (e^x-1)/x, phi2(x) = (e^x-1-x)/x^2."""
+    t = np.asarray(times, dtype=np.float64)
+    g = np.asarray(gf_t, dtype=np.complex128)
+    z = np.asarray(z, dtype=np.complex128)
+    u = 1j * z[:, None]
+    h = np.diff(t)[None, :]
+    x = u * h
+    small = np.abs(x) < 0.25
+    xs = np.where(small, 1.0, x)
+    phi1 = np.where(small, 0, (np.exp(xs) - 1) / xs)
+    phi2 = np.where(small, 0, (np.exp(xs) - 1 - xs) / xs**2)
+    if np.any(small):
+        a = np.zeros_like(x)
+        b = np.zeros_like(x)
+        fact1, fact2 = 1.0, 1.0
+        for k in range(17):  # Taylor: phi1 = sum x^k/(k+1)!, phi2 = sum x^k/(k+2)!
+            fact1 *= k + 1
+            fact2 *= k + 2
+            a = a + x**k / fact1
+            b = b + x**k / fact2
+        phi1 = np.where(small, a, phi1)
+        phi2 = np.where(small, b, phi2)
+    ej = np.exp(u * t[None, :-1])
+    seg = h * ej * (g[None, :-1] * phi2 + g[None, 1:] * (phi1 - phi2))
+    return seg.sum(axis=1)
+
+
+# ---- G_ij: lehmann_full.py:19-97 ---------------------------------------------------------------
+
+
+def _sector_dense(n_sites, desc, nu, nd):
+    eps, u, bonds, width = desc
+    up, dn = sector_states(n_sites, nu), sector_states(n_sites, nd)
+    r, c, v = coo_fermion(up, dn, eps, u, bonds, width)
+    return dense_from_coo(len(up) * len(dn), r, c, v), up, dn
+
+
+def greens_lehmann_draft(n_sites, desc, z, beta, i, j, sigma=UP):
+    """The reference's draft greens_lehmann (lehmann_full.py:48-97) as written: the sector
+    loop variable `i` shadows the site argument, so the annihilator acts on site = sector index
+    (lehmann_full.py:67,88); the overlap is |<n|c_pos|m>|^2 (lehmann_full.py:20-21); the sum is
+    not divided by the partition function. j does not enter."""
+    z = np.asarray(z, dtype=np.complex128)
+    gf = np.zeros_like(z)
+    e0 = np.inf
+    fillings = [(a, b) for a in range(n_sites + 1) for b in range(n_sites + 1)]
+    for idx, (n_up, n_dn) in enumerate(fillings):
+        up_t = n_up + 1 if sigma == UP else n_up
+        dn_t = n_dn + 1 if sigma != UP else n_dn
+        if up_t > n_sites or dn_t > n_sites:
+            continue
+        H, up, dn = _sector_dense(n_sites, desc, n_up, n_dn)
+        Hp, upp, dnp = _sector_dense(n_sites, desc, up_t, dn_t)
+        w, V = np.linalg.eigh(H)
+        wp, Vp = np.linalg.eigh(Hp)
+        min_energy = w.min()
+        factor = 1.0
+        if min_energy < e0:
+            factor = np.exp(-beta * (e0 - min_energy))
+            e0 = min_energy
+        if factor != 1.0:
+            gf *= factor
+        pos = idx  # the shadowed loop variable
+        if pos < n_sites:
+            # c_pos |m> for every eigenvector m of the upper sector, projected on <n|
+            c_m = apply_fermion(upp, dnp, up, dn, pos, sigma, False, Vp)
+            ov = (V.T @ c_m) ** 2  # [n, m]
+        else:
+            ov = np.zeros((len(w), len(wp)))
+        if np.isfinite(beta):
+            en, em = np.exp(-beta * (w - e0)), np.exp(-beta * (wp - e0))
+        else:
+            en, em = np.ones_like(w), np.ones_like(wp)
+        for m in range(len(wp)):
+            for n in range(len(w)):
+                gf += ov[n, m] * (en[n] + em[m]) / (z - wp[m] + w[n])
+    return gf
+
+
+def gf_offdiag_dense(n_sites, desc, z, beta, i, j, sigma=UP):
+    """Thermal G_ij(z) = Z^-1 sum <n|c_i|m><m|c^dag_j|n> (e^{-beta E_n} + e^{-beta E_m}) /
+    (z - E_m + E_n) over all sectors having an upper sector (the completed lehmann_full.py:19-45,
+    normalised like GreensFunctionMeasurement, exactdiag.py:137-212)."""
+    z = np.asarray(z, dtype=np.complex128)
+    terms = []
+    e0 = np.inf
+    for n_up in range(n_sites + 1):
+        for n_dn in range(n_sites + 1):
+            up_t = n_up + 1 if sigma == UP else n_up
+            dn_t = n_dn + 1 if sigma != UP else n_dn
+            if up_t > n_sites or dn_t > n_sites:
+                continue
+            H, up, dn = _sector_dense(n_sites, desc, n_up, n_dn)
+            Hp, upp, dnp = _sector_dense(n_sites, desc, up_t, dn_t)
+            w, V = np.linalg.eigh(H)
+            wp, Vp = np.linalg.eigh(Hp)
+            ai = Vp.T @ apply_fermion(up, dn, upp, dnp, i, sigma, True, V)
+            aj = Vp.T @ apply_fermion(up, dn, upp, dnp, j, sigma, True, V)
+            terms.append((w, wp, ai * aj))
+            e0 = min(e0, w.min())
+    gf = np.zeros_like(z)
+    part = 0.0
+    for w, wp, ov in terms:
+        en, em = np.exp(-beta * (w - e0)), np.exp(-beta * (wp - e0))
+        part += en.sum()
+        pole = wp[:, None] - w[None, :]
+        coef = ov * (en[None, :] + em[:, None])
+        gf += (coef.reshape(-1)[None, :] / (z[:, None] - pole.reshape(-1)[None, :])).sum(axis=1)
+    return gf / part

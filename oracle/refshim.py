@@ -165,6 +165,8 @@ def import_reference(path: Path | str = DEFAULT_REFERENCE):
     if not (path / "cmpy" / "__init__.py").exists():
         raise FileNotFoundError(f"no cmpy checkout at {path}")
     _install_stubs()
+    # the checkout is read-only input: never write bytecode caches next to its sources
+    sys.dont_write_bytecode = True
     if str(path) not in sys.path:
         sys.path.insert(0, str(path))
     import cmpy  # noqa: F401

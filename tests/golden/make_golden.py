@@ -172,6 +172,36 @@ def main(ref_path):
     e_t, v_t = R.exactdiag.lanczos_ground_state(a, bb)
     ed["tri_a"], ed["tri_b"], ed["tri_e"], ed["tri_v"] = a, bb, np.float64(e_t), v_t
     np.savez_compressed(HERE / "exactdiag.npz", **ed)
+
+    # 5. real-time Green's functions (exactdiag.py:248-301, scipy expm_multiply inside); the
+    #    ground state the reference used is stored so the engine evaluates the same input
+    tv = {}
+    for tag, model, t1, num in (("chain4_U2", m4, 20.0, 201), ("chain6_U4", m6, 8.0, 81), ("siam3", ms2, 10.0, 101)):
+        gsr = R.exactdiag.compute_groundstate(model)
+        times, gg = R.exactdiag.gf_greater(model, gsr, 0.0, t1, num, pos=0)
+        _, gl = R.exactdiag.gf_lesser(model, gsr, 0.0, t1, num, pos=0)
+        tv[f"{tag}_times"] = np.asarray(times)
+        tv[f"{tag}_greater"] = np.asarray(gg)
+        tv[f"{tag}_lesser"] = np.asarray(gl)
+        tv[f"{tag}_e0"] = np.float64(gsr.energy)
+        tv[f"{tag}_state"] = np.asarray(gsr.state, dtype=np.float64)
+        tv[f"{tag}_sector"] = np.array([gsr.n_up, gsr.n_dn])
+    np.savez_compressed(HERE / "tevo.npz", **tv)
+
+    # 6. the G_ij draft lehmann_full.py:48-97 (a script module beside the package)
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("lehmann_full", str(Path(ref_path) / "lehmann_full.py"))
+    lf = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(lf)
+    lh = {}
+    zl = np.linspace(-4, 4, 64) + 0.1j
+    lh["z"] = zl
+    for beta in (5.0, np.inf):
+        for i, j in ((0, 0), (0, 1), (1, 2)):
+            tag = f"chain4_U2_b{'inf' if not np.isfinite(beta) else int(beta)}_{i}{j}"
+            lh[tag] = np.asarray(lf.greens_lehmann(m4, zl, beta, i, j))
+    np.savez_compressed(HERE / "lehmann_full.npz", **lh)
     for f in sorted(HERE.glob("*.npz")):
         print(f"{f.name}: {f.stat().st_size / 1024:.1f} KiB")
 
