@@ -462,9 +462,11 @@ __host__ __device__ inline Mv3Layout mv3_layout(int64_t nd, int n_b2, int max_up
   auto al = [](size_t v) { return (v + 127) & ~(size_t)127; };
   Mv3Layout L;
   L.lstride = ((max_up + 3) & ~3) + 4;
-  L.raw_off = 0;                                                   // [MV3_R][nd] landing rows
-  L.xs_off = al(L.raw_off + (size_t)MV3_R * nd * 8);               // [nd + 1][MV3_R] interleaved
-  L.tab_off = al(L.xs_off + (size_t)(nd + 1) * MV3_R * 8);         // [n_b2][nd] slot pairs
+  // xs2 first: its base is the (constant) start of dynamic shared memory, so a gather address
+  // is the table's byte offset plus an immediate
+  L.xs_off = 0;                                                    // [nd + 1][MV3_R] interleaved
+  L.raw_off = al(L.xs_off + (size_t)(nd + 1) * MV3_R * 8);         // [MV3_R][nd] landing rows
+  L.tab_off = al(L.raw_off + (size_t)MV3_R * nd * 8);              // [n_b2][nd] slot pairs
   L.lst_off = al(L.tab_off + (size_t)n_b2 * nd * 4);               // [2][MV3_R][lstride]
   L.cnt_off = al(L.lst_off + (size_t)2 * MV3_R * L.lstride * 4);   // [2][MV3_R][4]
   L.bar_off = al(L.cnt_off + (size_t)2 * MV3_R * 4 * 4);
@@ -745,17 +747,20 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
         const longlong2 xo = xs2[c];
         int64_t h0 = corr0 * xo.x + (half ? up_hi[0] : up_lo[0]);
         int64_t h1 = corr1 * xo.y + (half ? up_hi[1] : up_lo[1]);
-        // dn neighbours: two bonds per table word, + rows then - rows; slot nd reads zeros
+        // dn neighbours: two bonds per table word (byte offsets into xs2), + rows then - rows;
+        // offset 16*nd reads zeros
         const uint32_t* tc = tab + c;
         for (int p = 0; p < n_b2pos; ++p) {
           const uint32_t w = tc[(int64_t)p * nd];
-          const longlong2 va = xs2[w & 0xffffu], vb = xs2[w >> 16];
+          const longlong2 va = *(const longlong2*)((const char*)xs2 + (w & 0xffffu));
+          const longlong2 vb = *(const longlong2*)((const char*)xs2 + (w >> 16));
           h0 += va.x + vb.x;
           h1 += va.y + vb.y;
         }
         for (int p = n_b2pos; p < n_b2; ++p) {
           const uint32_t w = tc[(int64_t)p * nd];
-          const longlong2 va = xs2[w & 0xffffu], vb = xs2[w >> 16];
+          const longlong2 va = *(const longlong2*)((const char*)xs2 + (w & 0xffffu));
+          const longlong2 vb = *(const longlong2*)((const char*)xs2 + (w >> 16));
           h0 -= va.x + vb.x;
           h1 -= va.y + vb.y;
         }
@@ -1147,8 +1152,10 @@ ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
   std::vector<uint32_t> btab2((size_t)std::max(n_rows / 2, 1) * nd);
   for (int pr = 0; pr < std::max(n_rows / 2, 1); ++pr)
     for (int64_t c = 0; c < nd; ++c)
-      btab2[(size_t)pr * nd + c] = (uint32_t)btab[(size_t)(2 * pr) * nd + c] |
-                                   ((uint32_t)btab[(size_t)(2 * pr + 1) * nd + c] << 16);
+      // byte offsets of the 16-byte interleaved row pair (slot * 16 < 2^16 needs nd < 4096; the
+      // kernel that reads this table is only chosen then)
+      btab2[(size_t)pr * nd + c] = ((uint32_t)btab[(size_t)(2 * pr) * nd + c] * 16u & 0xffffu) |
+                                   (((uint32_t)btab[(size_t)(2 * pr + 1) * nd + c] * 16u & 0xffffu) << 16);
   // diagonal bound in units of 2^-F, and the overflow guard
   //   |W| <= (max|diag| 2^F + hops * t_int) * 2^m_in < 2^62
   B.u_uniform = p->fp.u_uniform;
@@ -1275,8 +1282,9 @@ static int matvec_variant(const ed_plan_s* p) {
   const size_t optin = (size_t)p->ctx->smem_optin;
   const bool v2_ok = p->bfp.vec2 && v2_smem(p) + MV2_STATIC_SMEM <= optin && p->num_up >= 1;
   // list entries are int32 element offsets u * nd: the vector must have fewer than 2^31 elements
+  // (and the table holds 16-bit byte offsets: nd < 4096)
   const bool v3_ok = p->bfp.vec2 && p->bfp.dn_btab2 && v3_smem(p) + MV3_STATIC_SMEM <= optin && p->num_up >= 1 &&
-                     p->dim < ((int64_t)1 << 31);
+                     p->dim < ((int64_t)1 << 31) && p->num_dn < 4096;
   // two-pass (4): column panels of 4 (nd % 4 == 0), a panel of all rows in half the shared memory
   const bool v4_ok = v3_ok && p->num_dn % MV_PW == 0 && (size_t)p->num_up * MV_PW * 8 + 1024 <= optin / 2;
   if (forced == 1) return 1;

@@ -64,7 +64,8 @@ struct BfpTables {
   uint16_t* dn_tab = nullptr;
   // dn, bond-major: one row of partner columns per (bond, sign) that occurs, nd marking "no
   // hop" (a zero slot); + rows first, each sign class padded to an even count with zero rows;
-  // rows packed in pairs: [n_b2][nd] uint32 = slot(2p) | slot(2p+1) << 16
+  // rows packed in pairs as byte offsets into the interleaved row pair (16 bytes per column):
+  // [n_b2][nd] uint32 = 16*slot(2p) | 16*slot(2p+1) << 16
   uint32_t* dn_btab2 = nullptr;
   int n_b2 = 0, n_b2pos = 0;
   int max_up = 0;               // most up-neighbours of one row
