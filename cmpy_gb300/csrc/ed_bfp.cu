@@ -83,6 +83,17 @@ struct BfpVecs {
   __host__ __device__ __forceinline__ int64_t* vec(int k) const { return R + (int64_t)(store ? k : (k % 3)) * D; }
 };
 
+__device__ void bfp_scalars_tail(BfpVecs v, int k, int F, int m_in, double t, unsigned long long m, double* alpha,
+                                 const double* beta, BfpState* st);
+
+// Lanczos-step scalars folded into the last CTA of the matvec (when `on`)
+struct BfpFuse {
+  BfpVecs v;
+  int k, F, m_in, on;
+  double* alpha;
+  const double* beta;
+};
+
 constexpr int BT = 256;  // block size of the streaming kernels
 
 template <int NT>
@@ -586,7 +597,7 @@ template <bool DIAG64, bool UPW>
 __global__ void __launch_bounds__(MV3_MAXNT, 1)
     k_bfp_hub_matvec3(BfpHubArgs a, const uint32_t* __restrict__ btab2, int n_b2, int n_b2pos, int max_up,
                       const int64_t* __restrict__ X, int64_t* W, double* partial,
-                      unsigned long long* partial_max, BfpState* st, int* status) {
+                      unsigned long long* partial_max, BfpState* st, int* status, BfpFuse fz) {
   if (st && *(volatile int*)&st->stop) return;
   extern __shared__ __align__(128) unsigned char sm3[];
   __shared__ double smd[MV3_MAXNT / 32];
@@ -800,6 +811,21 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
     partial[blockIdx.x] = sdot;
     partial_max[blockIdx.x] = m;
   }
+  if (fz.on && st && bfp_last_block(&st->ticket[2])) {
+    // the last CTA to finish reduces the partials in CTA order and sets the step's scalars
+    double t = 0.0;
+    unsigned long long mm = 0;
+    for (int b = tid; b < (int)gridDim.x; b += nt) {
+      t += ((volatile double*)partial)[b];
+      mm = max(mm, ((volatile unsigned long long*)partial_max)[b]);
+    }
+    t = block_sum_rt(t, smd);
+    mm = block_max_rt(mm, smu);
+    if (tid == 0) {
+      bfp_scalars_tail(fz.v, fz.k, fz.F, fz.m_in, t, mm, fz.alpha, fz.beta, st);
+      st->ticket[2] = 0;
+    }
+  }
 }
 
 // ---- two-pass H·v, pass 1: up-neighbour sums by column panels ---------------------------------
@@ -879,6 +905,13 @@ __global__ void k_bfp_scalars(BfpVecs v, int k, int F, int m_in, const double* p
   t = block_sum<BT>(t, sm);
   m = block_max_u64<BT>(m, smu);
   if (threadIdx.x != 0) return;
+  bfp_scalars_tail(v, k, F, m_in, t, m, alpha, beta, st);
+}
+
+// alpha_k and the update coefficients from the reduced <R_k, W> (t, mantissa units) and
+// max|W| (m); one thread
+__device__ void bfp_scalars_tail(BfpVecs v, int k, int F, int m_in, double t, unsigned long long m, double* alpha,
+                                 const double* beta, BfpState* st) {
   const int ek = v.eR[k];
   const int ew = ek - F;
   const double bk = beta[k];
@@ -1326,7 +1359,7 @@ static ed_status launch_v2(const ed_plan_s* p, int g, const int64_t* X, int64_t*
 
 template <bool DIAG64, bool UPW>
 static ed_status launch_v3(const ed_plan_s* p, int g, const int64_t* X, int64_t* W, double* partial,
-                           unsigned long long* partial_max, BfpState* st, cudaStream_t s) {
+                           unsigned long long* partial_max, BfpState* st, cudaStream_t s, const BfpFuse& fz) {
   static std::atomic<uint64_t> done{0};
   const uint64_t bit = 1ull << (p->device & 63);
   if (!(done.load() & bit)) {
@@ -1349,7 +1382,7 @@ static ed_status launch_v3(const ed_plan_s* p, int g, const int64_t* X, int64_t*
   }
   k_bfp_hub_matvec3<DIAG64, UPW><<<g, v3_threads(p), v3_smem(p), s>>>(bfp_args(p), B.dn_btab2, B.n_b2, B.n_b2pos,
                                                                       B.max_up, X, W, partial, partial_max, st,
-                                                                      status);
+                                                                      status, fz);
   ED_CHECK_LAUNCH("k_bfp_hub_matvec3");
   return ED_OK;
 }
@@ -1370,8 +1403,14 @@ static ed_status launch_variant(const ed_plan_s* p, size_t smem, int g, const in
   return ED_OK;
 }
 
+// fz (optional): the Lanczos step whose scalars the matvec may compute in its last CTA;
+// *fused tells the caller whether it did (then no separate scalars kernel is needed)
 static ed_status launch_bfp_matvec(const ed_plan_s* p, const int64_t* X, int64_t* W, double* partial,
-                                   unsigned long long* partial_max, BfpState* st, cudaStream_t s) {
+                                   unsigned long long* partial_max, BfpState* st, cudaStream_t s,
+                                   const BfpFuse* fz = nullptr, bool* fused = nullptr) {
+  BfpFuse off{};
+  off.on = 0;
+  if (fused) *fused = false;
   const size_t smem = (2 * p->num_dn + 1) * sizeof(int64_t);
   const int g = bfp_matvec_grid(p);
   const bool d64 = p->bfp.diag64 != 0;
@@ -1380,12 +1419,15 @@ static ed_status launch_bfp_matvec(const ed_plan_s* p, const int64_t* X, int64_t
   // caller buffers take the one-column v1 kernel
   const bool aligned = (((uintptr_t)X | (uintptr_t)W) & 15) == 0;
   const int var = aligned ? matvec_variant(p) : 1;
-  if (var == 4)
-    return d64 ? launch_v3<true, true>(p, g, X, W, partial, partial_max, st, s)
-               : launch_v3<false, true>(p, g, X, W, partial, partial_max, st, s);
-  if (var == 3)
-    return d64 ? launch_v3<true, false>(p, g, X, W, partial, partial_max, st, s)
-               : launch_v3<false, false>(p, g, X, W, partial, partial_max, st, s);
+  if (var >= 3) {
+    const BfpFuse& f = (fz && partial && st) ? *fz : off;
+    if (fused) *fused = f.on != 0;
+    if (var == 4)
+      return d64 ? launch_v3<true, true>(p, g, X, W, partial, partial_max, st, s, f)
+                 : launch_v3<false, true>(p, g, X, W, partial, partial_max, st, s, f);
+    return d64 ? launch_v3<true, false>(p, g, X, W, partial, partial_max, st, s, f)
+               : launch_v3<false, false>(p, g, X, W, partial, partial_max, st, s, f);
+  }
   if (var == 2)
     return d64 ? launch_v2<true>(p, g, X, W, partial, partial_max, st, s)
                : launch_v2<false>(p, g, X, W, partial, partial_max, st, s);
@@ -1516,12 +1558,27 @@ static ed_status launch_update(const ed_plan_s* p, BfpRun& r, int k, double* alp
 }
 
 // one Lanczos step k: matvec + scalars + update (3 launches)
+static BfpFuse bfp_fuse(const ed_plan_s* p, const BfpRun& r, int k, double* alpha, const double* beta) {
+  BfpFuse f;
+  f.v = r.v;
+  f.k = k;
+  f.F = p->bfp.F;
+  f.m_in = p->bfp.m_in;
+  f.on = 1;
+  f.alpha = alpha;
+  f.beta = beta;
+  return f;
+}
+
 static ed_status bfp_step(const ed_plan_s* p, BfpRun& r, int k, double* alpha, double* beta, cudaStream_t s) {
   const int gmv = bfp_matvec_grid(p);
-  ED_TRY(launch_bfp_matvec(p, r.v.vec(k), r.W, r.part, r.partmax, r.st, s));
-  k_bfp_scalars<<<1, BT, 0, s>>>(r.v, k, p->bfp.F, p->bfp.m_in, r.part, r.partmax, gmv, alpha, beta, r.st);
+  const BfpFuse fz = bfp_fuse(p, r, k, alpha, beta);
+  bool fused = false;
+  ED_TRY(launch_bfp_matvec(p, r.v.vec(k), r.W, r.part, r.partmax, r.st, s, &fz, &fused));
+  if (!fused)
+    k_bfp_scalars<<<1, BT, 0, s>>>(r.v, k, p->bfp.F, p->bfp.m_in, r.part, r.partmax, gmv, alpha, beta, r.st);
   ED_TRY(launch_update(p, r, k, alpha, beta, s));
-  ED_CHECK_LAUNCH_N("bfp step", 2);
+  ED_CHECK_LAUNCH_N("bfp step", fused ? 1 : 2);
   return ED_OK;
 }
 
@@ -1551,12 +1608,15 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
   }
   for (int k = 0; k < Km; ++k) {
     if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k], s));
-    ED_TRY(launch_bfp_matvec(p, r.v.vec(k), r.W, r.part, r.partmax, r.st, s));
+    const BfpFuse fz = bfp_fuse(p, r, k, alpha, beta);
+    bool fused = false;
+    ED_TRY(launch_bfp_matvec(p, r.v.vec(k), r.W, r.part, r.partmax, r.st, s, &fz, &fused));
     if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k + 1], s));
-    k_bfp_scalars<<<1, BT, 0, s>>>(r.v, k, p->bfp.F, p->bfp.m_in, r.part, r.partmax, bfp_matvec_grid(p), alpha,
-                                   beta, r.st);
+    if (!fused)
+      k_bfp_scalars<<<1, BT, 0, s>>>(r.v, k, p->bfp.F, p->bfp.m_in, r.part, r.partmax, bfp_matvec_grid(p), alpha,
+                                     beta, r.st);
     ED_TRY(launch_update(p, r, k, alpha, beta, s));
-    uint64_t nl = 2;
+    uint64_t nl = fused ? 1 : 2;
     if (prm->check_every > 0 && ((k + 1) % prm->check_every == 0) && k + 1 < Km) {
       k_lz_check_bfp<<<1, 256, 0, s>>>(alpha, beta, k, prm->tol, r.st, r.c, r.work);
       ++nl;
