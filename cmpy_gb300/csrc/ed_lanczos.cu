@@ -124,50 +124,69 @@ __global__ void k_lz_update(double* __restrict__ w, const double* __restrict__ q
 }
 
 // ---- full reorthogonalisation: classical Gram-Schmidt against Q[0..m) -----------------------
-// partial[j*gridDim + b] = sum_{i in block b} Q[j][i] w[i]; the last block reduces into h[j].
-constexpr int RO_J = 8;  // basis vectors per pass over the w chunk
+// h = Q^T w. Block b owns the element chunk [b*ch, (b+1)*ch) (ch = ceil(n / gridDim)); each warp
+// forms whole dot products of that chunk with vectors j = warp, warp + nwarps, ... (four FMA
+// chains per lane, shuffle reduction), partial[j*gridDim + b]; the last block to finish sums
+// the partials of every j in block order. No block-wide barrier per vector.
 __global__ void k_multidot(const double* __restrict__ Q, int64_t ldq, int m, const double* __restrict__ w, int64_t n,
                            double* partial, double* h, LzState* st) {
   if (lz_stopped(st)) return;
-  __shared__ double sm[LZ_NT / 32];
-  for (int j0 = 0; j0 < m; j0 += RO_J) {
-    double acc[RO_J];
-#pragma unroll
-    for (int r = 0; r < RO_J; ++r) acc[r] = 0.0;
-    for (int64_t i = blockIdx.x * (int64_t)LZ_NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * LZ_NT) {
-      const double wi = w[i];
-#pragma unroll
-      for (int r = 0; r < RO_J; ++r)
-        if (j0 + r < m) acc[r] = fma(Q[(int64_t)(j0 + r) * ldq + i], wi, acc[r]);
+  const int64_t ch = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * ch;
+  const int64_t len = max((int64_t)0, min(n, i0 + ch) - i0);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const double* wc = w + i0;
+  for (int j = warp; j < m; j += nw) {
+    const double* q = Q + (int64_t)j * ldq + i0;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int64_t i = lane;
+    for (; i + 96 < len; i += 128) {
+      a0 = fma(__ldg(q + i), __ldg(wc + i), a0);
+      a1 = fma(__ldg(q + i + 32), __ldg(wc + i + 32), a1);
+      a2 = fma(__ldg(q + i + 64), __ldg(wc + i + 64), a2);
+      a3 = fma(__ldg(q + i + 96), __ldg(wc + i + 96), a3);
     }
+    for (; i < len; i += 32) a0 = fma(__ldg(q + i), __ldg(wc + i), a0);
+    double acc = (a0 + a1) + (a2 + a3);
 #pragma unroll
-    for (int r = 0; r < RO_J; ++r) {
-      const double s = block_sum<LZ_NT>(acc[r], sm);
-      if (threadIdx.x == 0 && j0 + r < m) partial[(int64_t)(j0 + r) * gridDim.x + blockIdx.x] = s;
-    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) partial[(int64_t)j * gridDim.x + blockIdx.x] = acc;
   }
   if (last_block(&st->ticket[2])) {
-    for (int j = 0; j < m; ++j) {
-      const double s = block_sum_array(partial + (int64_t)j * gridDim.x, gridDim.x, sm);
-      if (threadIdx.x == 0) h[j] = s;
+    for (int j = warp; j < m; j += nw) {
+      double acc = 0.0;
+      for (int b = lane; b < (int)gridDim.x; b += 32) acc += ((volatile double*)partial)[(int64_t)j * gridDim.x + b];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) h[j] = acc;
     }
     if (threadIdx.x == 0) st->ticket[2] = 0;
   }
 }
 
-// w -= sum_j h[j] Q[j]; optionally accumulates ||w||^2 and finalises beta_{k+1}
+// w -= sum_j h[j] Q[j] (four independent FMA chains per element); optionally accumulates ||w||^2
+// and finalises beta_{k+1}. m <= RO_MAX (checked by the host).
+constexpr int RO_MAX = 1024;
 __global__ void k_multiaxpy(const double* __restrict__ Q, int64_t ldq, int m, const double* __restrict__ h,
                             double* __restrict__ w, int64_t n, double* partial, LzState* st, double* beta_next,
                             int k, int final_norm, const double* alpha_k) {
   if (lz_stopped(st)) return;
   __shared__ double sm[LZ_NT / 32];
-  __shared__ double hs[1024];
-  for (int j = threadIdx.x; j < m && j < 1024; j += LZ_NT) hs[j] = h[j];
+  __shared__ double hs[RO_MAX];
+  for (int j = threadIdx.x; j < m; j += LZ_NT) hs[j] = h[j];
   __syncthreads();
   double v = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)LZ_NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * LZ_NT) {
-    double x = w[i];
-    for (int j = 0; j < m; ++j) x = fma(-hs[j], Q[(int64_t)j * ldq + i], x);
+    double x0 = w[i], x1 = 0.0, x2 = 0.0, x3 = 0.0;
+    int j = 0;
+    for (; j + 3 < m; j += 4) {
+      x0 = fma(-hs[j], __ldg(Q + (int64_t)j * ldq + i), x0);
+      x1 = fma(-hs[j + 1], __ldg(Q + (int64_t)(j + 1) * ldq + i), x1);
+      x2 = fma(-hs[j + 2], __ldg(Q + (int64_t)(j + 2) * ldq + i), x2);
+      x3 = fma(-hs[j + 3], __ldg(Q + (int64_t)(j + 3) * ldq + i), x3);
+    }
+    for (; j < m; ++j) x0 = fma(-hs[j], __ldg(Q + (int64_t)j * ldq + i), x0);
+    const double x = (x0 + x1) + (x2 + x3);
     w[i] = x;
     v = fma(x, x, v);
   }
@@ -367,6 +386,8 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
   }
   const int gv = nparts;
   const int gs = grid_for(D, 256, p->ctx->num_sms * 8);
+  // reorthogonalisation dots: element chunks of ~1024 (>= 32 elements per lane per vector)
+  const int gmd = (int)std::max<int64_t>(1, std::min<int64_t>((D + 1023) / 1024, nparts));
   auto qv = [&](int k) -> double* { return Q + (int64_t)(store ? k : (k % 3)) * D; };
   // q_0
   if (d_v0) {
@@ -407,7 +428,7 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
     uint64_t nl = 3;
     if (prm->reorth) {
       for (int pass = 0; pass < 2; ++pass) {
-        k_multidot<<<gv, LZ_NT, 0, s>>>(Q, D, k + 1, w, D, part, h, st);
+        k_multidot<<<gmd, LZ_NT, 0, s>>>(Q, D, k + 1, w, D, part, h, st);
         k_multiaxpy<<<gv, LZ_NT, 0, s>>>(Q, D, k + 1, h, w, D, part, st, d_beta + k + 1, k, pass == 1, d_alpha + k);
         nl += 2;
       }
