@@ -155,6 +155,11 @@ _SIGNATURES = {
     "ed_batch_gf_continued_fraction": (I32, [I32, I32, P, P, P, P, I32, P, I64, P, P]),
     "ed_plan_num_params": (I32, [PLAN]),
     "ed_param_sandwich": (I32, [PLAN, P, P, P, I32, P]),
+    "ed_tape_workspace": (I32, [PLAN, I32, I32, C.POINTER(C.c_size_t)]),
+    "ed_lanczos_tape": (I32, [PLAN, P, I32, I32, F64, I32, F64, P, C.c_size_t, P, P, P, C.POINTER(C.c_int), P]),
+    "ed_tape_combine": (I32, [PLAN, I32, I32, P, P, P, P, P, P, P, P, C.c_size_t, P]),
+    "ed_tape_reverse": (I32, [PLAN, I32, I32, P, P, P, P, P, P, P, P, C.c_size_t, P, P, P]),
+    "ed_cf_adjoint": (I32, [P, P, I32, F64, F64, I32, P, I64, P, P, P, P, P]),
     "ed_plan_fixed_point": (I32, [PLAN]),
     "ed_fixed_from_f64": (I32, [P, I64, I32, P, C.POINTER(C.c_int32), P]),
     "ed_fixed_to_f64": (I32, [P, I64, C.c_int32, P, P]),

@@ -9,18 +9,21 @@ theta = [eps_0..eps_{N-1}, U_0..U_{N-1}, t_0..t_{nb-1}] (the plan's order):
   2. phi = c^dag_{pos,sigma} psi0, chi = c_{pos,sigma} psi0;
   3. Lanczos of phi in the (n+1) sector and of chi in the (n-1) sector;
   4. G(z) = CF_particle(z) + CF_hole(z)  (continued fractions, z' = +-z + E0).
-Every Lanczos run stores only its scalars and the Krylov vectors q_k at k = 0 (mod c)
-(with q_{k-1}); the backward pass recomputes each segment of c vectors from its checkpoint
-with the stored (alpha, beta) (no reductions) and sweeps the adjoint recurrence backwards
-through it. Memory: about 2m/c + c vectors per run instead of m.
+Every Lanczos run is a native tape (ed_lanczos_tape): it keeps its scalars and the Krylov
+vectors q_k at k = 0 (mod c) (with q_{k-1}); the backward pass (ed_tape_reverse) recomputes
+each segment of c vectors from its checkpoint with the stored (alpha, beta), bit-identical to
+the forward, and sweeps the adjoint recurrence backwards through it. Memory: about 2m/c + 2c
+vectors per run instead of m. The host only enqueues kernels and reads m.
 
 Backward (exact reverse of the computed recurrences):
   * continued fraction: dG/dalpha_l, dG/dbeta_l, dG/dnorm^2, dG/dE0 by the chain through
     t_l = z' - alpha_l - beta_{l+1}^2 / t_{l+1};
   * Lanczos step k (w = H q_k, alpha = q.w, r = w - alpha q_k - beta_k q_{k-1},
     beta_{k+1} = ||r||, q_{k+1} = r / beta_{k+1}) reversed, with
-    theta_bar += wbar_k^T (dH/dtheta) q_k (ed_param_sandwich) and qbar_k += H wbar_k;
-  * Ritz vector and tridiagonal eigenpair: Tbar = Ebar c c^T + v c^T, v = -(T - E0)^+ cbar.
+    theta_bar += wbar_k^T (dH/dtheta) q_k (fused into the step's elementwise kernel) and
+    qbar_k += H wbar_k;
+  * Ritz vector and tridiagonal eigenpair: Tbar = Ebar c c^T + v c^T, v = -(T - E0)^+ cbar
+    (an m x m problem, solved on the host).
 Costs: forward = m0 + m_p + m_h matvecs; backward = one matvec per step for the segment
 recompute plus one for H wbar, i.e. about 2x the forward.
 """
@@ -28,7 +31,6 @@ recompute plus one for H wbar, i.e. about 2x the forward.
 from __future__ import annotations
 
 import ctypes as C
-import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -37,8 +39,8 @@ import torch
 from . import _native as N
 from . import engine as E
 
-__all__ = ["LanczosTape", "lanczos_taped", "lanczos_reverse", "greens_function_ad", "GreensFunctionAD",
-           "siam_parameters"]
+__all__ = ["Tape", "tape_forward", "tape_combine", "tape_reverse", "cf_adjoint", "greens_function_ad",
+           "GreensFunctionAD", "siam_parameters", "sandwich"]
 
 
 # ------------------------------------------------------------------------------------------
@@ -61,184 +63,108 @@ def sandwich(plan: E.Plan, a: torch.Tensor, b: torch.Tensor, out: torch.Tensor) 
 
 
 # ------------------------------------------------------------------------------------------
-# taped Lanczos (FP64): scalars + checkpoints
+# native tape: taped FP64 Lanczos, segment replay, reverse sweep (csrc/ed_adjoint.cu)
 # ------------------------------------------------------------------------------------------
 
 
 @dataclass
-class LanczosTape:
-    alpha: torch.Tensor   # [m]
-    beta: torch.Tensor    # [m+1]; beta[0] = ||start||, beta[k] couplings, beta[m] residual
-    ckpt: dict            # k -> (q_{k-1} or None, q_k) for k = 0 (mod c)
-    c: int
+class Tape:
+    """A taped Lanczos run of `plan`: alpha[m], beta[m+1] (beta[0] = ||start||), the
+    checkpoint pairs [q_{k-1}, q_k] for k = 0 (mod c), and the shared workspace."""
+    plan: E.Plan
+    alpha: torch.Tensor
+    beta: torch.Tensor
+    ckpt: torch.Tensor
     m: int
+    c: int
+    work: torch.Tensor
 
 
-def _lowest_ritz_residual(alpha, beta):
-    m = len(alpha)
-    a = torch.stack(alpha).cpu().numpy()
-    b = torch.stack(beta).cpu().numpy()
-    T = np.diag(a) + np.diag(b[1:m], 1) + np.diag(b[1:m], -1)
-    w, V = np.linalg.eigh(T)
-    return abs(b[m] * V[m - 1, 0]), w[0]
+def _workspace(plan: E.Plan, steps: int, c: int) -> torch.Tensor:
+    nb = C.c_size_t()
+    N.check(N.lib().ed_tape_workspace(plan.handle, int(steps), int(c), C.byref(nb)))
+    return torch.empty(int(nb.value), dtype=torch.uint8, device=E.device())
 
 
-def lanczos_taped(plan: E.Plan, start: torch.Tensor, m: int, c: int = 16, breakdown: float = 1e-13,
-                  tol: float = 0.0, check_every: int = 10) -> LanczosTape:
-    """Plain Lanczos from `start` keeping (alpha, beta) and checkpoints every c steps. With
-    tol > 0 it stops once the lowest Ritz pair has residual <= tol * max(1, |E|) (before
-    ghost copies of the converged value appear in T).
-
-    The recurrence runs in blocks of `check_every` steps without host synchronisation; the
-    breakdown test (beta_{k+1} <= breakdown * (|alpha_k| + beta_k)) and the convergence test
-    read the block's scalars once. Steps computed after a breakdown inside a block are
-    discarded, so the tape is the same as with a per-step test."""
-    s = start.reshape(-1)
-    b0 = torch.linalg.norm(s)
-    q = s / b0
-    qp = None
-    alpha, beta = [], [b0]
-    ckpt = {}
-    m = int(min(m, plan.dim))
-    blk = max(1, int(check_every))
-    stop = None
-    k = 0
-    while k < m and stop is None:
-        k_end = min(m, k + blk)
-        for kk in range(k, k_end):
-            if kk % c == 0:
-                ckpt[kk] = (qp, q)
-            w = plan.matvec(q)
-            a = torch.dot(q, w)
-            r = w - a * q
-            if qp is not None:
-                r = r - beta[kk] * qp
-            bn = torch.linalg.norm(r)
-            alpha.append(a)
-            beta.append(bn)
-            qp, q = q, r / bn  # inf/nan after an exact breakdown: those steps are dropped below
-        a_h = torch.stack(alpha[k:k_end]).cpu().numpy()
-        b_h = torch.stack(beta[k:k_end + 1]).cpu().numpy()
-        for j in range(k, k_end):
-            scale = abs(a_h[j - k]) + (b_h[j - k] if j > 0 else 0.0)
-            if not b_h[j - k + 1] > breakdown * scale:
-                stop = j + 1
-                break
-        if stop is None and tol > 0 and k_end % blk == 0:
-            res, e = _lowest_ritz_residual(alpha, beta)
-            if res <= tol * max(1.0, abs(e)):
-                stop = k_end
-        k = k_end
-    mm = stop if stop is not None else len(alpha)
-    ckpt = {kk: v for kk, v in ckpt.items() if kk < mm}
-    return LanczosTape(torch.stack(alpha[:mm]), torch.stack(beta[:mm + 1]), ckpt, c, mm)
+def tape_forward(plan: E.Plan, start: torch.Tensor, max_steps: int, c: int = 16, tol: float = 0.0,
+                 check_every: int = 10, breakdown: float = 1e-13) -> Tape | None:
+    """Taped Lanczos from `start` (None for a zero start vector). Stops on breakdown and,
+    with tol > 0, once the lowest Ritz pair has residual <= tol * max(1, |E|)."""
+    with plan._dev():
+        s = start.reshape(-1).to(dtype=torch.float64).contiguous()
+        K = int(min(max_steps, plan.dim))
+        work = _workspace(plan, K, c)
+        alpha = torch.empty(K, dtype=torch.float64, device=E.device())
+        beta = torch.empty(K + 1, dtype=torch.float64, device=E.device())
+        ckpt = torch.empty(((K + c - 1) // c, 2, plan.dim), dtype=torch.float64, device=E.device())
+        steps = C.c_int()
+        N.check(N.lib().ed_lanczos_tape(plan.handle, N.ptr(s), K, int(c), float(tol), int(check_every),
+                                        float(breakdown), N.ptr(work), work.numel(), N.ptr(alpha), N.ptr(beta),
+                                        N.ptr(ckpt), C.byref(steps), E._stream()))
+        m = int(steps.value)
+        if m == 0:
+            return None
+        return Tape(plan, alpha[:m], beta[:m + 1], ckpt, m, int(c), work)
 
 
-def _segment(plan, tape: LanczosTape, k0: int, k1: int):
-    """q_{k0-1} .. q_{k1} recomputed from the checkpoint at k0 with the stored scalars; the
-    vector after the last step (never used by the Green's function) is left at zero."""
-    qp, q = tape.ckpt[k0]
-    qs = {k0 - 1: qp, k0: q}
-    for k in range(k0, k1):
-        if k + 1 >= tape.m:
-            qs[k + 1] = torch.zeros_like(q)
-            continue
-        w = plan.matvec(qs[k])
-        r = w - tape.alpha[k] * qs[k]
-        if k > 0:
-            r = r - tape.beta[k] * qs[k - 1]
-        qs[k + 1] = r / tape.beta[k + 1]
-    return qs
+def tape_combine(tape: Tape, coef: torch.Tensor | None = None, probe: torch.Tensor | None = None):
+    """Replays the tape: (sum_k coef_k q_k or None, [q_k . probe]_k or None)."""
+    p = tape.plan
+    with p._dev():
+        out = torch.empty(p.dim, dtype=torch.float64, device=E.device()) if coef is not None else None
+        dots = torch.empty(tape.m, dtype=torch.float64, device=E.device()) if probe is not None else None
+        cf = coef.to(dtype=torch.float64).contiguous() if coef is not None else None
+        pr = probe.reshape(-1).to(dtype=torch.float64).contiguous() if probe is not None else None
+        N.check(N.lib().ed_tape_combine(p.handle, tape.m, tape.c, N.ptr(tape.alpha), N.ptr(tape.beta),
+                                        N.ptr(tape.ckpt), N.ptr(cf), N.ptr(out), N.ptr(pr), N.ptr(dots),
+                                        N.ptr(tape.work), tape.work.numel(), E._stream()))
+        return out, dots
 
 
-def lanczos_reverse(plan: E.Plan, tape: LanczosTape, abar: torch.Tensor, bbar: torch.Tensor,
-                    qbar_ext: dict | None, theta_bar: torch.Tensor) -> torch.Tensor:
-    """Reverse sweep of the taped recurrence. abar[m], bbar[m+1] (bbar[0]: adjoint of the
-    start norm), qbar_ext: extra adjoints of q_k (k -> vector). Accumulates the parameter
-    gradient into theta_bar and returns the adjoint of the start vector."""
-    m = tape.m
-    abar = abar.clone()
-    bbar = bbar.clone()
-    qbar = {}  # adjoints of q_k, filled as the sweep descends
-    if qbar_ext:
-        for k, v in qbar_ext.items():
-            qbar[k] = v.clone()
-    seg_starts = sorted(tape.ckpt)
-    for s0 in reversed(seg_starts):
-        s1 = min(s0 + tape.c, m)
-        qs = _segment(plan, tape, s0, s1)  # q_{s0-1} .. q_{s1}
-        for k in range(s1 - 1, s0 - 1, -1):
-            qk, qkp1 = qs[k], qs[k + 1]
-            bk1 = tape.beta[k + 1]
-            qb_next = qbar.pop(k + 1, None)
-            # q_{k+1} = r_k / beta_{k+1} ; beta_{k+1} = ||r_k||
-            if qb_next is not None:
-                rbar = qb_next / bk1
-                bbar[k + 1] = bbar[k + 1] - torch.dot(qb_next, qkp1) / bk1
-            else:
-                rbar = torch.zeros_like(qk)
-            rbar = rbar + bbar[k + 1] * qkp1
-            # r_k = w_k - alpha_k q_k - beta_k q_{k-1}
-            w = plan.matvec(qk)
-            abar[k] = abar[k] - torch.dot(rbar, qk)
-            qb = qbar.get(k, torch.zeros_like(qk)) - tape.alpha[k] * rbar
-            if k > 0:
-                bbar[k] = bbar[k] - torch.dot(rbar, qs[k - 1])
-                qbar[k - 1] = qbar.get(k - 1, torch.zeros_like(qk)) - tape.beta[k] * rbar
-            # alpha_k = q_k . w_k
-            wbar = rbar + abar[k] * qk
-            qb = qb + abar[k] * w
-            # w_k = H q_k
-            sandwich(plan, wbar, qk, theta_bar)
-            qb = qb + plan.matvec(wbar)
-            qbar[k] = qb
-    q0 = tape.ckpt[0][1]
-    qb0 = qbar.get(0, torch.zeros_like(q0))
-    b0 = tape.beta[0]
-    # q_0 = s / ||s||, beta_0 = ||s||
-    return (qb0 - torch.dot(qb0, q0) * q0) / b0 + bbar[0] * q0
+def tape_reverse(tape: Tape, abar: torch.Tensor, bbar: torch.Tensor, theta_bar: torch.Tensor,
+                 ext_coef: torch.Tensor | None = None, ext_vec: torch.Tensor | None = None) -> torch.Tensor:
+    """Reverse sweep: accumulates dL/dtheta into theta_bar, returns dL/dstart. abar[m] and
+    bbar[m+1] are the adjoints of the tape's scalars (bbar[0]: of ||start||); the Krylov
+    vectors get the external adjoints q_bar_k += ext_coef[k] * ext_vec."""
+    p = tape.plan
+    with p._dev():
+        ab = abar.to(dtype=torch.float64).contiguous()
+        bb = bbar.to(dtype=torch.float64).contiguous()
+        ec = ext_coef.to(dtype=torch.float64).contiguous() if ext_coef is not None else None
+        ev = ext_vec.reshape(-1).to(dtype=torch.float64).contiguous() if ext_vec is not None else None
+        sbar = torch.empty(p.dim, dtype=torch.float64, device=E.device())
+        N.check(N.lib().ed_tape_reverse(p.handle, tape.m, tape.c, N.ptr(tape.alpha), N.ptr(tape.beta),
+                                        N.ptr(tape.ckpt), N.ptr(ab), N.ptr(bb), N.ptr(ec), N.ptr(ev),
+                                        N.ptr(tape.work), tape.work.numel(), N.ptr(theta_bar), N.ptr(sbar),
+                                        E._stream()))
+        return sbar
 
 
-# ------------------------------------------------------------------------------------------
-# continued fraction with its derivatives
-# ------------------------------------------------------------------------------------------
-
-
-def cf_eval(alpha, beta, n2, z, e0, sign):
-    """G(z) and the per-level quantities needed for its derivatives (torch, complex128)."""
-    m = alpha.numel()
-    zp = sign * z + e0
-    ts = [None] * m
-    t = zp - alpha[m - 1]
-    ts[m - 1] = t
-    for l in range(m - 2, -1, -1):
-        t = zp - alpha[l] - beta[l + 1] ** 2 / t
-        ts[l] = t
-    g = sign * n2 / ts[0]
-    return g, ts
-
-
-def cf_adjoint(alpha, beta, n2, z, e0, sign, gbar):
+def cf_adjoint(alpha: torch.Tensor, beta: torch.Tensor, n2: float, z: torch.Tensor, e0: float, sign: int,
+               gbar: torch.Tensor):
     """Adjoints (abar[m], bbar[m+1] with bbar[0] for sqrt(n2), e0bar) of
-    L = Re sum conj(gbar) G."""
+    L = Re sum conj(gbar) G for G = sign n2 / (z' - alpha_0 - beta_1^2 / ...), z' = sign z + e0."""
     m = alpha.numel()
-    g, ts = cf_eval(alpha, beta, n2, z, e0, sign)
-    u = -sign * n2 / ts[0] ** 2  # dG/dt_0
-    abar = torch.zeros(m, dtype=torch.float64, device=alpha.device)
-    bbar = torch.zeros(m + 1, dtype=torch.float64, device=alpha.device)
-    dz = torch.zeros_like(u)
-    cg = torch.conj(gbar)
-    for l in range(m):
-        dz = dz + u  # dt_l/dz' = 1
-        abar[l] = torch.real(torch.sum(cg * (-u)))
-        if l + 1 < m:
-            bb = beta[l + 1]
-            bbar[l + 1] = torch.real(torch.sum(cg * (u * (-2.0 * bb / ts[l + 1]))))
-            u = u * (bb * bb) / ts[l + 1] ** 2
-    e0bar = torch.real(torch.sum(cg * dz))
-    n2bar = torch.real(torch.sum(cg * (sign / ts[0])))
-    bbar[0] = n2bar * 2.0 * torch.sqrt(n2)  # norm adjoint
-    return g, abar, bbar, e0bar
+    abar = torch.empty(m, dtype=torch.float64, device=E.device())
+    bbar = torch.empty(m + 1, dtype=torch.float64, device=E.device())
+    scal = torch.empty(2, dtype=torch.float64, device=E.device())
+    zt = E._as_dev_c128(z)
+    gb = E._as_dev_c128(gbar)
+    N.check(N.lib().ed_cf_adjoint(N.ptr(alpha), N.ptr(beta), m, float(n2), float(e0), int(sign),
+                                  N.ptr(torch.view_as_real(zt)), zt.numel(), N.ptr(torch.view_as_real(gb)),
+                                  N.ptr(abar), N.ptr(bbar), N.ptr(scal), E._stream()))
+    return abar, bbar, scal[0]
+
+
+def _tridiag_lowest_host(a: np.ndarray, b: np.ndarray):
+    """Lowest eigenpair of the tridiagonal (a[0..m), b[1..m)), LAPACK on the host."""
+    from scipy.linalg import eigh_tridiagonal
+
+    m = a.size
+    if m == 1:
+        return float(a[0]), np.ones(1)
+    w, v = eigh_tridiagonal(a, b[1:m], select="i", select_range=(0, 0))
+    return float(w[0]), v[:, 0]
 
 
 # ------------------------------------------------------------------------------------------
@@ -255,19 +181,13 @@ class GreensFunctionAD(torch.autograd.Function):
         plan = plan_from_params(theta, n_sites, bonds, width, nu, nd)
         gen = torch.Generator(device="cpu").manual_seed(seed)
         v0 = torch.rand(plan.dim, generator=gen, dtype=torch.float64).to(E.device())
-        tape0 = lanczos_taped(plan, v0, m0, c, tol=1e-12)
+        tape0 = tape_forward(plan, v0, m0, c, tol=1e-12)
         m = tape0.m
-        T = torch.diag(tape0.alpha) + torch.diag(tape0.beta[1:m], 1) + torch.diag(tape0.beta[1:m], -1)
-        w, V = torch.linalg.eigh(T)
-        e0 = w[0]
-        cvec = V[:, 0]
-        # Ritz vector (segments recomputed from checkpoints)
-        y = torch.zeros(plan.dim, dtype=torch.float64, device=E.device())
-        for s0 in sorted(tape0.ckpt):
-            s1 = min(s0 + tape0.c, m)
-            qs = _segment(plan, tape0, s0, s1)
-            for k in range(s0, s1):
-                y = y + cvec[k] * qs[k]
+        a_h = tape0.alpha.cpu().numpy()
+        b_h = tape0.beta.cpu().numpy()
+        e0, cvec_h = _tridiag_lowest_host(a_h, b_h)
+        cvec = torch.as_tensor(cvec_h, dtype=torch.float64).to(E.device())
+        y, _ = tape_combine(tape0, coef=cvec)
         ynorm = torch.linalg.norm(y)
         psi = y / ynorm
         zt = E._as_dev_c128(z)
@@ -280,58 +200,55 @@ class GreensFunctionAD(torch.autograd.Function):
                 continue
             tp = plan_from_params(theta, n_sites, bonds, width, tu, td)
             start = plan.apply_fermion(tp, pos, sigma, create, psi)
-            if torch.linalg.norm(start).item() == 0.0:
+            tape = tape_forward(tp, start, mgf, c)
+            if tape is None:
                 parts.append(None)
                 continue
-            tape = lanczos_taped(tp, start, mgf, c)
-            n2 = tape.beta[0] ** 2
-            gp, _ = cf_eval(tape.alpha, tape.beta, n2, zt, e0, sign)
-            g = g + gp
-            parts.append((tp, tape, sign, create))
-        ctx.saved = (plan, tape0, cvec, w, ynorm, psi, e0, zt, parts, spec)
+            n2 = float(tape.beta[0].item()) ** 2
+            E.continued_fraction(tape.alpha, tape.beta, n2, zt, e0, sign, out=g)
+            parts.append((tp, tape, sign, create, n2))
+        ctx.saved = (plan, tape0, cvec_h, e0, ynorm, psi, zt, parts, spec)
         return g
 
     @staticmethod
     def backward(ctx, gbar):
-        plan, tape0, cvec, w, ynorm, psi, e0, zt, parts, spec = ctx.saved
+        plan, tape0, cvec_h, e0, ynorm, psi, zt, parts, spec = ctx.saved
         n_sites, bonds, width, (nu, nd), pos, sigma, m0, mgf, c, seed = spec
         P = 2 * n_sites + len(bonds)
         theta_bar = torch.zeros(P, dtype=torch.float64, device=E.device())
-        e0bar = torch.zeros((), dtype=torch.float64, device=E.device())
+        e0bar = 0.0
         psibar = torch.zeros_like(psi)
+        gb = gbar.to(E.device()).contiguous()
         for part in parts:
             if part is None:
                 continue
-            tp, tape, sign, create = part
-            n2 = tape.beta[0] ** 2
-            _, abar, bbar, eb = cf_adjoint(tape.alpha, tape.beta, n2, zt, e0, sign, gbar)
-            e0bar = e0bar + eb
-            sbar = lanczos_reverse(tp, tape, abar, bbar, None, theta_bar)
+            tp, tape, sign, create, n2 = part
+            abar, bbar, eb = cf_adjoint(tape.alpha, tape.beta, n2, zt, e0, sign, gb)
+            e0bar += float(eb.item())
+            sbar = tape_reverse(tape, abar, bbar, theta_bar)
             # start = c^dag psi (or c psi): its adjoint maps back with the opposite operator
             psibar = psibar + tp.apply_fermion(plan, pos, sigma, not create, sbar)
         # psi = y / ||y||, y = sum_k c_k q_k
         ybar = (psibar - torch.dot(psibar, psi) * psi) / ynorm
         m = tape0.m
-        # c_bar_k = q_k . ybar and the external q_bar_k = c_k ybar, segment by segment
-        cbar = torch.zeros(m, dtype=torch.float64, device=E.device())
-        for s0 in sorted(tape0.ckpt):
-            s1 = min(s0 + tape0.c, m)
-            qs = _segment(plan, tape0, s0, s1)
-            for k in range(s0, s1):
-                cbar[k] = torch.dot(qs[k], ybar)
-        # eigenpair of T: E0 = c^T T c, c = ground state of T
-        T = torch.diag(tape0.alpha) + torch.diag(tape0.beta[1:m], 1) + torch.diag(tape0.beta[1:m], -1)
-        cb = cbar - torch.dot(cbar, cvec) * cvec
-        A = T - w[0] * torch.eye(m, dtype=torch.float64, device=E.device())
-        # v = -(T - E0)^+ cb on the complement of c (add c c^T to make the system regular)
-        v = -torch.linalg.solve(A + torch.outer(cvec, cvec), cb)
-        v = v - torch.dot(v, cvec) * cvec
+        _, cbar_d = tape_combine(tape0, probe=ybar)
+        cbar = cbar_d.cpu().numpy()
+        cvec = cvec_h
+        # eigenpair of T: E0 = c^T T c, c = ground state of T; v = -(T - E0)^+ cbar on the
+        # complement of c (c c^T added to make the system regular)
+        a_h = tape0.alpha.cpu().numpy()
+        b_h = tape0.beta.cpu().numpy()
+        T = np.diag(a_h) + np.diag(b_h[1:m], 1) + np.diag(b_h[1:m], -1)
+        cb = cbar - np.dot(cbar, cvec) * cvec
+        v = -np.linalg.solve(T - e0 * np.eye(m) + np.outer(cvec, cvec), cb)
+        v = v - np.dot(v, cvec) * cvec
         abar0 = e0bar * cvec ** 2 + v * cvec
-        bbar0 = torch.zeros(m + 1, dtype=torch.float64, device=E.device())
+        bbar0 = np.zeros(m + 1)
         if m > 1:
             bbar0[1:m] = 2.0 * e0bar * cvec[:-1] * cvec[1:] + v[:-1] * cvec[1:] + v[1:] * cvec[:-1]
-        qext = {k: cvec[k] * ybar for k in range(m)}
-        lanczos_reverse(plan, tape0, abar0, bbar0, qext, theta_bar)
+        dev = E.device()
+        tape_reverse(tape0, torch.as_tensor(abar0).to(dev), torch.as_tensor(bbar0).to(dev), theta_bar,
+                     ext_coef=torch.as_tensor(cvec).to(dev), ext_vec=ybar)
         return theta_bar.to(gbar.device), None, None
 
 

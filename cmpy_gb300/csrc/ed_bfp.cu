@@ -1474,7 +1474,7 @@ size_t bfp_workspace_bytes(const ed_plan_s* p, int K, bool store) { return bfp_l
 __global__ void k_lz_check_bfp(const double* alpha, const double* beta, int k, double tol, BfpState* st, double* c,
                                double* work) {
   if (*(volatile int*)&st->stop) return;
-  const double e = tridiag_lowest_block(alpha, beta, k + 1, c, work);
+  const double e = tridiag_lowest_block<512>(alpha, beta, k + 1, c, work);
   if (threadIdx.x == 0) {
     const double res = fabs(beta[k + 1] * c[k]);
     if (res <= tol * fmax(1.0, fabs(e))) { st->stop = 1; st->steps = k + 1; }
@@ -1487,7 +1487,7 @@ __global__ void k_lz_check_bfp(const double* alpha, const double* beta, int k, d
 __global__ void k_lz_final_bfp(const double* alpha, const double* beta, int kmax, BfpState* st, double* c,
                                double* work) {
   const int m = st->stop ? st->steps : kmax;
-  const double e = tridiag_lowest_block(alpha, beta, m, c, work);
+  const double e = tridiag_lowest_block<512>(alpha, beta, m, c, work);
   if (threadIdx.x == 0) {
     st->energy = e;
     st->steps = m;

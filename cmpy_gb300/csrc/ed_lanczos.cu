@@ -212,7 +212,7 @@ __global__ void k_multiaxpy(const double* __restrict__ Q, int64_t ldq, int m, co
 __global__ void k_lz_check(const double* alpha, const double* beta, int k, double tol, LzState* st, double* c,
                            double* work) {
   if (lz_stopped(st)) return;
-  const double e = tridiag_lowest_block(alpha, beta, k + 1, c, work);
+  const double e = tridiag_lowest_block<512>(alpha, beta, k + 1, c, work);
   if (threadIdx.x == 0) {
     const double res = fabs(beta[k + 1] * c[k]);
     if (res <= tol * fmax(1.0, fabs(e))) { st->stop = 1; st->steps = k + 1; }
@@ -225,7 +225,7 @@ __global__ void k_lz_check(const double* alpha, const double* beta, int k, doubl
 // final eigenpair of T_m; m = st->steps if stopped else kmax
 __global__ void k_lz_final(const double* alpha, const double* beta, int kmax, LzState* st, double* c, double* work) {
   const int m = st->stop ? st->steps : kmax;
-  const double e = tridiag_lowest_block(alpha, beta, m, c, work);
+  const double e = tridiag_lowest_block<512>(alpha, beta, m, c, work);
   if (threadIdx.x == 0) {
     st->energy = e;
     st->steps = m;
@@ -234,7 +234,7 @@ __global__ void k_lz_final(const double* alpha, const double* beta, int kmax, Lz
 }
 
 __global__ void k_tridiag(const double* alpha, const double* beta, int m, double* value, double* vec, double* work) {
-  const double e = tridiag_lowest_block(alpha, beta, m, vec, work);
+  const double e = tridiag_lowest_block<512>(alpha, beta, m, vec, work);
   if (threadIdx.x == 0) *value = e;
 }
 

@@ -47,7 +47,7 @@ static ed_status scratch_address(double** out) {
 
 __global__ void k_tridiag_noalloc(const double* alpha, const double* beta, int m, double* value, double* vec,
                                   double* work) {
-  const double e = tridiag_lowest_block(alpha, beta, m, vec, work);
+  const double e = tridiag_lowest_block<512>(alpha, beta, m, vec, work);
   if (threadIdx.x == 0) *value = e;
 }
 

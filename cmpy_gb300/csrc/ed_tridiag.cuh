@@ -39,9 +39,37 @@ static __device__ int sturm_count(const double* a, const double* b, int m, doubl
 // scarce pipe on this GPU, so fewer points per round cost less in total), then optionally
 // the eigenvector by inverse iteration (thread 0, FP64, partial pivoting).
 constexpr int MS_PTS = 32;
-static __device__ double tridiag_lowest_block(const double* a, const double* b, int m, double* vec, double* work) {
+//
+// SM_M > 0 (single-block callers): for m <= SM_M the tridiagonal, the elimination work and the
+// vector live in static shared memory (7 * SM_M doubles) instead of global memory, which takes
+// the inverse iteration's dependent loads off the L2 round trip. Batched callers keep SM_M = 0.
+template <int SM_M = 0>
+static __device__ double tridiag_lowest_block(const double* a_g, const double* b_g, int m, double* vec_g,
+                                              double* work_g) {
   __shared__ double lo_s, hi_s;
   __shared__ int cnt_s[MS_PTS];
+  const double* a = a_g;
+  const double* b = b_g;
+  double* vec = vec_g;
+  double* work = work_g;
+  bool in_smem = false;
+  if constexpr (SM_M > 0) {
+    __shared__ double s_ab[2 * SM_M];
+    __shared__ double s_w[5 * SM_M];
+    __shared__ double s_v[SM_M];
+    if (m <= SM_M) {
+      for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        s_ab[i] = a_g[i];
+        s_ab[SM_M + i] = b_g[i];
+      }
+      __syncthreads();
+      a = s_ab;
+      b = s_ab + SM_M;
+      work = s_w;
+      if (vec_g) vec = s_v;
+      in_smem = true;
+    }
+  }
   if (threadIdx.x == 0) {
     double lo = a[0], hi = a[0];
     for (int i = 0; i < m; ++i) {
@@ -132,6 +160,10 @@ static __device__ double tridiag_lowest_block(const double* a, const double* b, 
     for (int i = 0; i < m; ++i) vec[i] *= sg;
   }
   __syncthreads();
+  if (in_smem && vec_g) {
+    for (int i = threadIdx.x; i < m; i += blockDim.x) vec_g[i] = vec[i];
+    __syncthreads();
+  }
   return ev;
 }
 

@@ -316,6 +316,45 @@ ED_API int ed_plan_num_params(ed_plan plan);
 ED_API ed_status ed_param_sandwich(ed_plan plan, const double* d_a, const double* d_b, double* d_out,
                                    int accumulate, ed_stream_t stream);
 
+/* Taped FP64 Lanczos for reverse mode. The plain three-term recurrence of cmpy's Lanczos
+ * coefficients (cmpy/exactdiag.py:324-365), normalised, from d_start: alpha[0..m),
+ * beta[0..m] (beta[0] = ||start||, beta[m] the last residual norm). Every ckpt-th step k
+ * stores [q_{k-1}, q_k] in d_ckpt + (k/ckpt)*2*D (q_{-1} = 0): ceil(min(max_steps, D)/ckpt)
+ * slots of 2*D doubles. Stops on breakdown (beta_{k+1} <= breakdown*(|alpha_k| + beta_k))
+ * and, with tol > 0, when the lowest Ritz pair has |beta_{k+1} c_k| <= tol*max(1, |E|)
+ * (tested every check_every steps; the host reads the stop flag then). Synchronous; h_steps
+ * = m (0 for a zero start vector). Fermionic plans; workspace from ed_tape_workspace
+ * (shared by the three tape calls). */
+ED_API ed_status ed_tape_workspace(ed_plan plan, int max_steps, int ckpt, size_t* bytes);
+ED_API ed_status ed_lanczos_tape(ed_plan plan, const double* d_start, int max_steps, int ckpt,
+                                 double tol, int check_every, double breakdown, void* d_work,
+                                 size_t work_bytes, double* d_alpha, double* d_beta,
+                                 double* d_ckpt, int* h_steps, ed_stream_t stream);
+/* Replays a tape segment by segment from its checkpoints (bit-identical Krylov vectors):
+ * d_out = sum_{k<m} d_coef[k] q_k (the Ritz vector) and/or d_dots[k] = q_k . d_probe. */
+ED_API ed_status ed_tape_combine(ed_plan plan, int m, int ckpt, const double* d_alpha,
+                                 const double* d_beta, const double* d_ckpt, const double* d_coef,
+                                 double* d_out, const double* d_probe, double* d_dots,
+                                 void* d_work, size_t work_bytes, ed_stream_t stream);
+/* Reverse sweep of a tape: given the adjoints of the scalars (d_abar[m], d_bbar[m+1], d_bbar[0]
+ * for ||start||) and optional external adjoints of the Krylov vectors q_bar_k +=
+ * d_ext_coef[k] * d_ext_vec, accumulates d_theta_bar[p] += dL/dtheta_p (parameter layout of
+ * ed_plan_num_params) and writes the adjoint of the start vector to d_start_bar. Each
+ * segment is recomputed from its checkpoint; two matvecs per step. */
+ED_API ed_status ed_tape_reverse(ed_plan plan, int m, int ckpt, const double* d_alpha,
+                                 const double* d_beta, const double* d_ckpt, const double* d_abar,
+                                 const double* d_bbar, const double* d_ext_coef,
+                                 const double* d_ext_vec, void* d_work, size_t work_bytes,
+                                 double* d_theta_bar, double* d_start_bar, ed_stream_t stream);
+/* Adjoint of the continued fraction of ed_gf_continued_fraction: for
+ * L = Re sum_j conj(gbar_j) G(z_j) (d_z, d_gbar interleaved complex), d_abar[l] = dL/dalpha_l,
+ * d_bbar[l] = dL/dbeta_l (l = 1..m-1; d_bbar[0] = dL/d sqrt(norm2), d_bbar[m] = 0),
+ * d_scal[0] = dL/dshift, d_scal[1] = dL/dnorm2. */
+ED_API ed_status ed_cf_adjoint(const double* d_alpha, const double* d_beta, int m, double norm2,
+                               double shift, int sign, const double* d_z, int64_t n_z,
+                               const double* d_gbar, double* d_abar, double* d_bbar,
+                               double* d_scal, ed_stream_t stream);
+
 /* ---- block-fixed-point vectors (no reference counterpart: GB300 arithmetic) ------------
  * A vector is stored as int64 mantissas m[i] with one exponent e: x[i] = m[i] * 2^e. On
  * GB300 the FP64 pipe is ~60x narrower than the integer pipe, so the engine's fast matvec
