@@ -438,38 +438,58 @@ def run_disorder_batch(n_real: int = 512, n_freq: int = 1024):
     }
 
 
-def run_adjoint(n_siam: int = 64, n_freq: int = 1024):
-    """Adjoint: SIAMs with 1 impurity + 9 bath sites (star), U=4, eps_d=-U/2, sector (5,5);
-    G_imp(i w_n) on n_freq Matsubara frequencies (beta=100) and the adjoint gradient of a
-    least-squares loss against a target hybridisation with 30 poles, w.r.t. bath energies and V."""
+def run_adjoint(n_siam: int = 64, n_freq: int = 1024, n_single: int = 8, workers: int = 8):
+    """Adjoint: SIAMs with 1 impurity + 9 bath sites (star), U=4, eps_d=-U/2, sector (5,5)
+    (eps_bath ~ U[-2,2], V ~ U[0.1,0.6], numpy default_rng(5)); G_imp(i w_n) on n_freq
+    Matsubara frequencies (beta=100) and the adjoint gradient of a least-squares loss against a
+    target hybridisation with 30 poles, w.r.t. bath energies and V. Single problems (forward /
+    backward cost, after one warm-up) and all n_siam SIAMs at once on `workers` streams."""
     import torch
 
-    from cmpy_gb300.adjoint import greens_function_ad, siam_parameters
+    from cmpy_gb300.adjoint import greens_function_ad, greens_function_ad_batch, siam_parameters
 
     rng = np.random.default_rng(5)
     ek = rng.uniform(-2, 2, 30)
     z = 1j * (2 * np.arange(n_freq) + 1) * np.pi / 100.0
     gt = torch.as_tensor(1.0 / (z - np.sum(0.3**2 / (z[:, None] - ek[None, :]), axis=1))).cuda()
+    eb = torch.tensor(rng.uniform(-2, 2, (n_siam, 9)), dtype=torch.float64, device="cuda", requires_grad=True)
+    v = torch.tensor(rng.uniform(0.1, 0.6, (n_siam, 9)), dtype=torch.float64, device="cuda", requires_grad=True)
+    u = torch.tensor(4.0, dtype=torch.float64, device="cuda")
+    e_imp = torch.tensor(0.0, dtype=torch.float64, device="cuda")
+    kw = dict(gs_steps=250, gf_levels=150, ckpt=16)
+
+    def thetas():
+        rows = [siam_parameters(u, e_imp, eb[i], v[i]) for i in range(n_siam)]
+        return torch.stack([r[0] for r in rows]), rows[0][1], rows[0][2], rows[0][3]
+
+    th, n_sites, bonds, width = thetas()
     fwd, bwd = [], []
-    for s in range(n_siam + 1):  # the first SIAM is a warm-up (lazy kernel loading), not timed
-        eb = torch.tensor(rng.uniform(-2, 2, 9), dtype=torch.float64, device="cuda", requires_grad=True)
-        v = torch.tensor(rng.uniform(0.1, 0.6, 9), dtype=torch.float64, device="cuda", requires_grad=True)
-        u = torch.tensor(4.0, dtype=torch.float64, device="cuda")
-        theta, n_sites, bonds, width = siam_parameters(u, torch.tensor(0.0, dtype=torch.float64, device="cuda"), eb, v)
-        g, tf = _timed(lambda: greens_function_ad(theta, n_sites, bonds, (5, 5), z, sign_width=width, gs_steps=250,
-                                                   gf_levels=150, ckpt=16))
+    for s in range(n_single + 1):  # the first is a warm-up (lazy kernel loading), not timed
+        g, tf = _timed(lambda: greens_function_ad(th[s % n_siam], n_sites, bonds, (5, 5), z, sign_width=width, **kw))
         loss = torch.sum(torch.abs(g - gt) ** 2)
-        _, tb = _timed(lambda: loss.backward())
+        _, tb = _timed(lambda: loss.backward(retain_graph=True))
         if s > 0:
             fwd.append(tf)
             bwd.append(tb)
+    eb.grad = None
+    v.grad = None
+    th, n_sites, bonds, width = thetas()
+    gall, tbf = _timed(lambda: greens_function_ad_batch(th, n_sites, bonds, (5, 5), z, sign_width=width,
+                                                        workers=workers, **kw))
+    lall = torch.sum(torch.abs(gall - gt) ** 2)
+    _, tbb = _timed(lambda: lall.backward())
     return {
         "workload": f"siam_1p9_sector55_matsubara{n_freq}_beta100",
-        "siams_timed": n_siam,
+        "single_timed": n_single,
         "forward_ms": round(float(np.mean(fwd)), 2),
         "backward_ms": round(float(np.mean(bwd)), 2),
         "backward_over_forward": round(float(np.mean(bwd) / np.mean(fwd)), 3),
-        "gradients_per_s": round(1e3 / float(np.mean(fwd) + np.mean(bwd)), 2),
+        "batch_siams": n_siam,
+        "batch_workers": workers,
+        "batch_forward_ms": round(tbf, 1),
+        "batch_backward_ms": round(tbb, 1),
+        "batch_gradients_per_s": round(n_siam * 1e3 / (tbf + tbb), 1),
+        "single_gradients_per_s": round(1e3 / float(np.mean(fwd) + np.mean(bwd)), 1),
     }
 
 

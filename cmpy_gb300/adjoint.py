@@ -40,7 +40,7 @@ from . import _native as N
 from . import engine as E
 
 __all__ = ["Tape", "tape_forward", "tape_combine", "tape_reverse", "cf_adjoint", "greens_function_ad",
-           "GreensFunctionAD", "siam_parameters", "sandwich"]
+           "greens_function_ad_batch", "GreensFunctionAD", "GreensFunctionADBatch", "siam_parameters", "sandwich"]
 
 
 # ------------------------------------------------------------------------------------------
@@ -172,84 +172,148 @@ def _tridiag_lowest_host(a: np.ndarray, b: np.ndarray):
 # ------------------------------------------------------------------------------------------
 
 
+def _gf_forward(theta: torch.Tensor, spec, zt: torch.Tensor, g: torch.Tensor):
+    """Forward of one problem on the current stream: adds G(z) into g, returns what the
+    backward needs."""
+    n_sites, bonds, width, (nu, nd), pos, sigma, m0, mgf, c, seed = spec
+    plan = plan_from_params(theta, n_sites, bonds, width, nu, nd)
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    v0 = torch.rand(plan.dim, generator=gen, dtype=torch.float64).to(E.device())
+    tape0 = tape_forward(plan, v0, m0, c, tol=1e-12)
+    a_h = tape0.alpha.cpu().numpy()
+    b_h = tape0.beta.cpu().numpy()
+    e0, cvec_h = _tridiag_lowest_host(a_h, b_h)
+    cvec = torch.as_tensor(cvec_h, dtype=torch.float64).to(E.device())
+    y, _ = tape_combine(tape0, coef=cvec)
+    ynorm = torch.linalg.norm(y)
+    psi = y / ynorm
+    parts = []
+    for delta, create, sign in ((1, True, 1), (-1, False, -1)):
+        tu, td = (nu + delta, nd) if sigma == 1 else (nu, nd + delta)
+        if not (0 <= tu <= n_sites and 0 <= td <= n_sites):
+            parts.append(None)
+            continue
+        tp = plan_from_params(theta, n_sites, bonds, width, tu, td)
+        start = plan.apply_fermion(tp, pos, sigma, create, psi)
+        tape = tape_forward(tp, start, mgf, c)
+        if tape is None:
+            parts.append(None)
+            continue
+        n2 = float(tape.beta[0].item()) ** 2
+        E.continued_fraction(tape.alpha, tape.beta, n2, zt, e0, sign, out=g)
+        parts.append((tp, tape, sign, create, n2))
+    return (plan, tape0, a_h, b_h, cvec_h, e0, ynorm, psi, zt, parts, spec)
+
+
+def _gf_backward(saved, gbar: torch.Tensor) -> torch.Tensor:
+    """Backward of one problem on the current stream: dL/dtheta for L = Re sum conj(gbar) G."""
+    plan, tape0, a_h, b_h, cvec, e0, ynorm, psi, zt, parts, spec = saved
+    n_sites, bonds, width, (nu, nd), pos, sigma, m0, mgf, c, seed = spec
+    P = 2 * n_sites + len(bonds)
+    theta_bar = torch.zeros(P, dtype=torch.float64, device=E.device())
+    e0bar = 0.0
+    psibar = torch.zeros_like(psi)
+    gb = gbar.to(E.device()).contiguous()
+    for part in parts:
+        if part is None:
+            continue
+        tp, tape, sign, create, n2 = part
+        abar, bbar, eb = cf_adjoint(tape.alpha, tape.beta, n2, zt, e0, sign, gb)
+        e0bar += float(eb.item())
+        sbar = tape_reverse(tape, abar, bbar, theta_bar)
+        # start = c^dag psi (or c psi): its adjoint maps back with the opposite operator
+        psibar = psibar + tp.apply_fermion(plan, pos, sigma, not create, sbar)
+    # psi = y / ||y||, y = sum_k c_k q_k
+    ybar = (psibar - torch.dot(psibar, psi) * psi) / ynorm
+    m = tape0.m
+    _, cbar_d = tape_combine(tape0, probe=ybar)
+    cbar = cbar_d.cpu().numpy()
+    # eigenpair of T: E0 = c^T T c, c = ground state of T; v = -(T - E0)^+ cbar on the
+    # complement of c (c c^T added to make the system regular)
+    T = np.diag(a_h) + np.diag(b_h[1:m], 1) + np.diag(b_h[1:m], -1)
+    cb = cbar - np.dot(cbar, cvec) * cvec
+    v = -np.linalg.solve(T - e0 * np.eye(m) + np.outer(cvec, cvec), cb)
+    v = v - np.dot(v, cvec) * cvec
+    abar0 = e0bar * cvec ** 2 + v * cvec
+    bbar0 = np.zeros(m + 1)
+    if m > 1:
+        bbar0[1:m] = 2.0 * e0bar * cvec[:-1] * cvec[1:] + v[:-1] * cvec[1:] + v[1:] * cvec[:-1]
+    dev = E.device()
+    tape_reverse(tape0, torch.as_tensor(abar0).to(dev), torch.as_tensor(bbar0).to(dev), theta_bar,
+                 ext_coef=torch.as_tensor(cvec).to(dev), ext_vec=ybar)
+    return theta_bar
+
+
 class GreensFunctionAD(torch.autograd.Function):
     """G(z) of a fermionic model sector as a differentiable function of theta."""
 
     @staticmethod
     def forward(ctx, theta, spec, z):
-        n_sites, bonds, width, (nu, nd), pos, sigma, m0, mgf, c, seed = spec
-        plan = plan_from_params(theta, n_sites, bonds, width, nu, nd)
-        gen = torch.Generator(device="cpu").manual_seed(seed)
-        v0 = torch.rand(plan.dim, generator=gen, dtype=torch.float64).to(E.device())
-        tape0 = tape_forward(plan, v0, m0, c, tol=1e-12)
-        m = tape0.m
-        a_h = tape0.alpha.cpu().numpy()
-        b_h = tape0.beta.cpu().numpy()
-        e0, cvec_h = _tridiag_lowest_host(a_h, b_h)
-        cvec = torch.as_tensor(cvec_h, dtype=torch.float64).to(E.device())
-        y, _ = tape_combine(tape0, coef=cvec)
-        ynorm = torch.linalg.norm(y)
-        psi = y / ynorm
         zt = E._as_dev_c128(z)
         g = torch.zeros_like(zt)
-        parts = []
-        for delta, create, sign in ((1, True, 1), (-1, False, -1)):
-            tu, td = (nu + delta, nd) if sigma == 1 else (nu, nd + delta)
-            if not (0 <= tu <= n_sites and 0 <= td <= n_sites):
-                parts.append(None)
-                continue
-            tp = plan_from_params(theta, n_sites, bonds, width, tu, td)
-            start = plan.apply_fermion(tp, pos, sigma, create, psi)
-            tape = tape_forward(tp, start, mgf, c)
-            if tape is None:
-                parts.append(None)
-                continue
-            n2 = float(tape.beta[0].item()) ** 2
-            E.continued_fraction(tape.alpha, tape.beta, n2, zt, e0, sign, out=g)
-            parts.append((tp, tape, sign, create, n2))
-        ctx.saved = (plan, tape0, cvec_h, e0, ynorm, psi, zt, parts, spec)
+        ctx.saved = _gf_forward(theta, spec, zt, g)
         return g
 
     @staticmethod
     def backward(ctx, gbar):
-        plan, tape0, cvec_h, e0, ynorm, psi, zt, parts, spec = ctx.saved
-        n_sites, bonds, width, (nu, nd), pos, sigma, m0, mgf, c, seed = spec
-        P = 2 * n_sites + len(bonds)
-        theta_bar = torch.zeros(P, dtype=torch.float64, device=E.device())
-        e0bar = 0.0
-        psibar = torch.zeros_like(psi)
-        gb = gbar.to(E.device()).contiguous()
-        for part in parts:
-            if part is None:
-                continue
-            tp, tape, sign, create, n2 = part
-            abar, bbar, eb = cf_adjoint(tape.alpha, tape.beta, n2, zt, e0, sign, gb)
-            e0bar += float(eb.item())
-            sbar = tape_reverse(tape, abar, bbar, theta_bar)
-            # start = c^dag psi (or c psi): its adjoint maps back with the opposite operator
-            psibar = psibar + tp.apply_fermion(plan, pos, sigma, not create, sbar)
-        # psi = y / ||y||, y = sum_k c_k q_k
-        ybar = (psibar - torch.dot(psibar, psi) * psi) / ynorm
-        m = tape0.m
-        _, cbar_d = tape_combine(tape0, probe=ybar)
-        cbar = cbar_d.cpu().numpy()
-        cvec = cvec_h
-        # eigenpair of T: E0 = c^T T c, c = ground state of T; v = -(T - E0)^+ cbar on the
-        # complement of c (c c^T added to make the system regular)
-        a_h = tape0.alpha.cpu().numpy()
-        b_h = tape0.beta.cpu().numpy()
-        T = np.diag(a_h) + np.diag(b_h[1:m], 1) + np.diag(b_h[1:m], -1)
-        cb = cbar - np.dot(cbar, cvec) * cvec
-        v = -np.linalg.solve(T - e0 * np.eye(m) + np.outer(cvec, cvec), cb)
-        v = v - np.dot(v, cvec) * cvec
-        abar0 = e0bar * cvec ** 2 + v * cvec
-        bbar0 = np.zeros(m + 1)
-        if m > 1:
-            bbar0[1:m] = 2.0 * e0bar * cvec[:-1] * cvec[1:] + v[:-1] * cvec[1:] + v[1:] * cvec[:-1]
-        dev = E.device()
-        tape_reverse(tape0, torch.as_tensor(abar0).to(dev), torch.as_tensor(bbar0).to(dev), theta_bar,
-                     ext_coef=torch.as_tensor(cvec).to(dev), ext_vec=ybar)
-        return theta_bar.to(gbar.device), None, None
+        return _gf_backward(ctx.saved, gbar).to(gbar.device), None, None
+
+
+def _on_workers(n: int, workers: int, fn) -> None:
+    """fn(i) for i < n on `workers` host threads, each with its own CUDA stream (problem i
+    always on stream i % workers); the calling stream is ordered before and after. The
+    library calls release the GIL, so the problems' kernel chains overlap on the GPU."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    main = torch.cuda.current_stream()
+    streams = [torch.cuda.Stream() for _ in range(workers)]
+
+    def run(w):
+        s = streams[w]
+        s.wait_stream(main)
+        with torch.cuda.stream(s):
+            for i in range(w, n, workers):
+                fn(i)
+
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        for f in [ex.submit(run, w) for w in range(workers)]:
+            f.result()
+    for s in streams:
+        main.wait_stream(s)
+
+
+class GreensFunctionADBatch(torch.autograd.Function):
+    """G(z) of B problems with the same structure (rows of theta), forward and backward spread
+    over worker threads and streams."""
+
+    @staticmethod
+    def forward(ctx, thetas, spec, z, workers):
+        zt = E._as_dev_c128(z)
+        B = thetas.shape[0]
+        g = torch.zeros((B, zt.numel()), dtype=torch.complex128, device=E.device())
+        saved = [None] * B
+
+        def fwd(i):
+            saved[i] = _gf_forward(thetas[i], spec, zt, g[i])
+
+        _on_workers(B, workers, fwd)
+        ctx.saved = saved
+        ctx.workers = workers
+        return g
+
+    @staticmethod
+    def backward(ctx, gbar):
+        saved = ctx.saved
+        B = len(saved)
+        P = 2 * saved[0][-1][0] + len(saved[0][-1][1])
+        out = torch.zeros((B, P), dtype=torch.float64, device=E.device())
+        gb = gbar.contiguous()
+
+        def bwd(i):
+            out[i].copy_(_gf_backward(saved[i], gb[i]))
+
+        _on_workers(B, ctx.workers, bwd)
+        return out.to(gbar.device), None, None, None
 
 
 def greens_function_ad(theta: torch.Tensor, n_sites: int, bonds, sector, z, pos: int = 0, sigma: int = 1,
@@ -259,6 +323,19 @@ def greens_function_ad(theta: torch.Tensor, n_sites: int, bonds, sector, z, pos:
     spec = (n_sites, [tuple(b) for b in bonds], n_sites if sign_width is None else sign_width, tuple(sector), pos,
             sigma, gs_steps, gf_levels, ckpt, seed)
     return GreensFunctionAD.apply(theta, spec, z)
+
+
+def greens_function_ad_batch(thetas: torch.Tensor, n_sites: int, bonds, sector, z, pos: int = 0, sigma: int = 1,
+                             sign_width: int | None = None, gs_steps: int = 200, gf_levels: int = 200,
+                             ckpt: int = 16, seed: int = 0, workers: int = 8) -> torch.Tensor:
+    """Differentiable T=0 G(z) of B models with one structure (thetas[B, P], rows as in
+    greens_function_ad) -> [B, n_z]. Each problem's arithmetic is that of greens_function_ad;
+    the problems run concurrently on `workers` CUDA streams."""
+    spec = (n_sites, [tuple(b) for b in bonds], n_sites if sign_width is None else sign_width, tuple(sector), pos,
+            sigma, gs_steps, gf_levels, ckpt, seed)
+    if thetas.dim() != 2:
+        raise ValueError("thetas must be [B, P]")
+    return GreensFunctionADBatch.apply(thetas, spec, z, max(1, min(int(workers), thetas.shape[0])))
 
 
 def siam_parameters(u, eps_imp, eps_bath, v, mu=None):

@@ -141,3 +141,37 @@ def test_adjoint_checkpoint_invariance(cuda):
         grads.append(torch.cat([eb.grad, v.grad]).cpu().numpy())
     np.testing.assert_allclose(grads[1], grads[0], rtol=1e-9, atol=1e-12)
     np.testing.assert_allclose(grads[2], grads[0], rtol=1e-9, atol=1e-12)
+
+
+def test_adjoint_batch_equals_single(cuda):
+    """greens_function_ad_batch (problems on several streams and host threads) gives each
+    problem exactly the forward and gradient of greens_function_ad."""
+    from cmpy_gb300.adjoint import greens_function_ad, greens_function_ad_batch
+
+    rng = np.random.default_rng(41)
+    B, nb = 5, 4
+    z = 1j * (2 * np.arange(40) + 1) * np.pi / 100.0
+    gt = torch.as_tensor(_target(z)).cuda()
+    eb0 = rng.uniform(-2, 2, (B, nb))
+    v0 = rng.uniform(0.1, 0.6, (B, nb))
+    kw = dict(gs_steps=150, gf_levels=100, ckpt=8)
+
+    eb = torch.tensor(eb0, dtype=torch.float64, device="cuda", requires_grad=True)
+    v = torch.tensor(v0, dtype=torch.float64, device="cuda", requires_grad=True)
+    rows = []
+    for i in range(B):
+        th, n_sites, bonds, width = _siam_theta(4.0, eb[i], v[i])
+        rows.append(th)
+    thetas = torch.stack(rows)
+    g = greens_function_ad_batch(thetas, n_sites, bonds, (2, 3), z, sign_width=width, workers=3, **kw)
+    _loss(g, gt.expand_as(g)).backward()
+
+    for i in range(B):
+        ebi = torch.tensor(eb0[i], dtype=torch.float64, device="cuda", requires_grad=True)
+        vi = torch.tensor(v0[i], dtype=torch.float64, device="cuda", requires_grad=True)
+        th, _, _, _ = _siam_theta(4.0, ebi, vi)
+        gi = greens_function_ad(th, n_sites, bonds, (2, 3), z, sign_width=width, **kw)
+        assert torch.equal(gi.detach(), g[i].detach())
+        _loss(gi, gt).backward()
+        assert torch.equal(ebi.grad, eb.grad[i])
+        assert torch.equal(vi.grad, v.grad[i])
