@@ -438,12 +438,12 @@ def run_disorder_batch(n_real: int = 512, n_freq: int = 1024):
     }
 
 
-def run_adjoint(n_siam: int = 64, n_freq: int = 1024, n_single: int = 8, workers: int = 8):
+def run_adjoint(n_siam: int = 64, n_freq: int = 1024, n_single: int = 8):
     """Adjoint: SIAMs with 1 impurity + 9 bath sites (star), U=4, eps_d=-U/2, sector (5,5)
     (eps_bath ~ U[-2,2], V ~ U[0.1,0.6], numpy default_rng(5)); G_imp(i w_n) on n_freq
     Matsubara frequencies (beta=100) and the adjoint gradient of a least-squares loss against a
     target hybridisation with 30 poles, w.r.t. bath energies and V. Single problems (forward /
-    backward cost, after one warm-up) and all n_siam SIAMs at once on `workers` streams."""
+    backward cost, after one warm-up) and all n_siam SIAMs at once (batched tape)."""
     import torch
 
     from cmpy_gb300.adjoint import greens_function_ad, greens_function_ad_batch, siam_parameters
@@ -474,8 +474,8 @@ def run_adjoint(n_siam: int = 64, n_freq: int = 1024, n_single: int = 8, workers
     eb.grad = None
     v.grad = None
     th, n_sites, bonds, width = thetas()
-    gall, tbf = _timed(lambda: greens_function_ad_batch(th, n_sites, bonds, (5, 5), z, sign_width=width,
-                                                        workers=workers, **kw))
+    greens_function_ad_batch(th[:2], n_sites, bonds, (5, 5), z, sign_width=width, **kw)  # warm-up
+    gall, tbf = _timed(lambda: greens_function_ad_batch(th, n_sites, bonds, (5, 5), z, sign_width=width, **kw))
     lall = torch.sum(torch.abs(gall - gt) ** 2)
     _, tbb = _timed(lambda: lall.backward())
     return {
@@ -485,7 +485,6 @@ def run_adjoint(n_siam: int = 64, n_freq: int = 1024, n_single: int = 8, workers
         "backward_ms": round(float(np.mean(bwd)), 2),
         "backward_over_forward": round(float(np.mean(bwd) / np.mean(fwd)), 3),
         "batch_siams": n_siam,
-        "batch_workers": workers,
         "batch_forward_ms": round(tbf, 1),
         "batch_backward_ms": round(tbb, 1),
         "batch_gradients_per_s": round(n_siam * 1e3 / (tbf + tbb), 1),

@@ -160,6 +160,17 @@ _SIGNATURES = {
     "ed_tape_combine": (I32, [PLAN, I32, I32, P, P, P, P, P, P, P, P, C.c_size_t, P]),
     "ed_tape_reverse": (I32, [PLAN, I32, I32, P, P, P, P, P, P, P, P, C.c_size_t, P, P, P]),
     "ed_cf_adjoint": (I32, [P, P, I32, F64, F64, I32, P, I64, P, P, P, P, P]),
+    "ed_batch_diag": (I32, [PLAN, I32, P, P, P]),
+    "ed_batch_cf": (I32, [I32, P, I64, P, I64, P, P, P, I32, P, I64, P, P]),
+    "ed_batch_cf_adjoint": (I32, [I32, P, I64, P, I64, P, I32, P, P, I32, P, I64, P, P, P, P, P]),
+    "ed_batch_matvec_params": (I32, [PLAN, I32, P, P, P, P, P]),
+    "ed_batch_tape_workspace": (I32, [PLAN, I32, I32, I32, C.POINTER(C.c_size_t)]),
+    "ed_batch_lanczos_tape": (I32, [PLAN, I32, P, P, P, I32, I32, F64, I32, F64, P, C.c_size_t, P, P, P,
+                                    C.POINTER(C.c_int), P]),
+    "ed_batch_tape_combine": (I32, [PLAN, I32, P, P, C.POINTER(C.c_int), I32, I32, P, P, P, P, P, P, P, P,
+                                    C.c_size_t, P]),
+    "ed_batch_tape_reverse": (I32, [PLAN, I32, P, P, C.POINTER(C.c_int), I32, I32, P, P, P, P, P, P, P, P,
+                                    C.c_size_t, P, P, P]),
     "ed_plan_fixed_point": (I32, [PLAN]),
     "ed_fixed_from_f64": (I32, [P, I64, I32, P, C.POINTER(C.c_int32), P]),
     "ed_fixed_to_f64": (I32, [P, I64, C.c_int32, P, P]),

@@ -40,7 +40,9 @@ from . import _native as N
 from . import engine as E
 
 __all__ = ["Tape", "tape_forward", "tape_combine", "tape_reverse", "cf_adjoint", "greens_function_ad",
-           "greens_function_ad_batch", "GreensFunctionAD", "GreensFunctionADBatch", "siam_parameters", "sandwich"]
+           "greens_function_ad_batch", "GreensFunctionAD", "GreensFunctionADBatch", "siam_parameters", "sandwich",
+           "BatchTape", "structure_plan", "batch_diag", "batch_matvec", "batch_tape_forward", "batch_tape_combine",
+           "batch_tape_reverse"]
 
 
 # ------------------------------------------------------------------------------------------
@@ -259,61 +261,243 @@ class GreensFunctionAD(torch.autograd.Function):
         return _gf_backward(ctx.saved, gbar).to(gbar.device), None, None
 
 
-def _on_workers(n: int, workers: int, fn) -> None:
-    """fn(i) for i < n on `workers` host threads, each with its own CUDA stream (problem i
-    always on stream i % workers); the calling stream is ordered before and after. The
-    library calls release the GIL, so the problems' kernel chains overlap on the GPU."""
-    from concurrent.futures import ThreadPoolExecutor
+# ------------------------------------------------------------------------------------------
+# batched native tape: B problems of one structure per launch (csrc/ed_adjoint_batch.cu)
+# ------------------------------------------------------------------------------------------
 
-    main = torch.cuda.current_stream()
-    streams = [torch.cuda.Stream() for _ in range(workers)]
 
-    def run(w):
-        s = streams[w]
-        s.wait_stream(main)
-        with torch.cuda.stream(s):
-            for i in range(w, n, workers):
-                fn(i)
+def structure_plan(n_sites: int, bonds, sign_width: int, n_up: int, n_dn: int) -> E.Plan:
+    """Plan of a sector with t = 1 on every bond and eps = U = 0: its hop coefficients are the
+    fermionic signs, the structure shared by every parameter set."""
+    z = np.zeros(n_sites)
+    return E.Plan.fermion(n_sites, z, z, [(i, j, 1.0) for (i, j) in bonds], n_up, n_dn, sign_width)
 
-    with ThreadPoolExecutor(max_workers=workers) as ex:
-        for f in [ex.submit(run, w) for w in range(workers)]:
-            f.result()
-    for s in streams:
-        main.wait_stream(s)
+
+@dataclass
+class BatchTape:
+    """B taped Lanczos runs of one structure: alpha[B, K], beta[B, K+1], checkpoints
+    [slot, 2, B, D], the tape lengths m[b] and the shared workspace."""
+    plan: E.Plan
+    thetas: torch.Tensor
+    diag: torch.Tensor
+    alpha: torch.Tensor
+    beta: torch.Tensor
+    ckpt: torch.Tensor
+    m: list
+    K: int
+    c: int
+    work: torch.Tensor
+
+
+def batch_diag(plan: E.Plan, thetas: torch.Tensor) -> torch.Tensor:
+    B = thetas.shape[0]
+    diag = torch.empty((B, plan.dim), dtype=torch.float64, device=E.device())
+    N.check(N.lib().ed_batch_diag(plan.handle, B, N.ptr(thetas), N.ptr(diag), E._stream()))
+    return diag
+
+
+def batch_matvec(plan: E.Plan, thetas: torch.Tensor, diag: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
+    """y[b] = H(theta_b) x[b]."""
+    y = torch.empty_like(x)
+    N.check(N.lib().ed_batch_matvec_params(plan.handle, thetas.shape[0], N.ptr(thetas), N.ptr(diag), N.ptr(x),
+                                           N.ptr(y), E._stream()))
+    return y
+
+
+def batch_tape_forward(plan: E.Plan, thetas: torch.Tensor, diag: torch.Tensor, starts: torch.Tensor, max_steps: int,
+                       c: int = 16, tol: float = 0.0, check_every: int = 10,
+                       breakdown: float = 1e-13) -> BatchTape:
+    B = thetas.shape[0]
+    K = int(min(max_steps, plan.dim))
+    nb = C.c_size_t()
+    N.check(N.lib().ed_batch_tape_workspace(plan.handle, B, K, int(c), C.byref(nb)))
+    work = torch.empty(int(nb.value), dtype=torch.uint8, device=E.device())
+    alpha = torch.empty((B, K), dtype=torch.float64, device=E.device())
+    beta = torch.empty((B, K + 1), dtype=torch.float64, device=E.device())
+    ckpt = torch.empty(((K + c - 1) // c, 2, B, plan.dim), dtype=torch.float64, device=E.device())
+    steps = (C.c_int * B)()
+    st = starts.to(dtype=torch.float64).contiguous()
+    N.check(N.lib().ed_batch_lanczos_tape(plan.handle, B, N.ptr(thetas), N.ptr(diag), N.ptr(st), K, int(c),
+                                          float(tol), int(check_every), float(breakdown), N.ptr(work), work.numel(),
+                                          N.ptr(alpha), N.ptr(beta), N.ptr(ckpt), steps, E._stream()))
+    return BatchTape(plan, thetas, diag, alpha, beta, ckpt, [int(v) for v in steps], K, int(c), work)
+
+
+def _hm(tape: BatchTape):
+    return (C.c_int * len(tape.m))(*tape.m)
+
+
+def batch_tape_combine(tape: BatchTape, coef: torch.Tensor | None = None, probe: torch.Tensor | None = None):
+    """Replays B tapes: (rows sum_k coef[b, k] q_k[b] or None, dots[b, k] = q_k[b] . probe[b] or None)."""
+    p, B = tape.plan, len(tape.m)
+    out = torch.empty((B, p.dim), dtype=torch.float64, device=E.device()) if coef is not None else None
+    dots = torch.zeros((B, tape.K), dtype=torch.float64, device=E.device()) if probe is not None else None
+    cf = coef.to(dtype=torch.float64).contiguous() if coef is not None else None
+    pr = probe.to(dtype=torch.float64).contiguous() if probe is not None else None
+    N.check(N.lib().ed_batch_tape_combine(p.handle, B, N.ptr(tape.thetas), N.ptr(tape.diag), _hm(tape), tape.K, tape.c,
+                                          N.ptr(tape.alpha), N.ptr(tape.beta), N.ptr(tape.ckpt), N.ptr(cf), N.ptr(out),
+                                          N.ptr(pr), N.ptr(dots), N.ptr(tape.work), tape.work.numel(), E._stream()))
+    return out, dots
+
+
+def batch_tape_reverse(tape: BatchTape, abar: torch.Tensor, bbar: torch.Tensor, theta_bar: torch.Tensor,
+                       ext_coef: torch.Tensor | None = None, ext_vec: torch.Tensor | None = None) -> torch.Tensor:
+    """Reverse sweep of B tapes: theta_bar[b] += dL/dtheta_b; returns dL/dstart [B, D]."""
+    p, B = tape.plan, len(tape.m)
+    ab = abar.to(dtype=torch.float64).contiguous()
+    bb = bbar.to(dtype=torch.float64).contiguous()
+    ec = ext_coef.to(dtype=torch.float64).contiguous() if ext_coef is not None else None
+    ev = ext_vec.to(dtype=torch.float64).contiguous() if ext_vec is not None else None
+    sbar = torch.empty((B, p.dim), dtype=torch.float64, device=E.device())
+    N.check(N.lib().ed_batch_tape_reverse(p.handle, B, N.ptr(tape.thetas), N.ptr(tape.diag), _hm(tape), tape.K,
+                                          tape.c, N.ptr(tape.alpha), N.ptr(tape.beta), N.ptr(tape.ckpt), N.ptr(ab),
+                                          N.ptr(bb), N.ptr(ec), N.ptr(ev), N.ptr(tape.work), tape.work.numel(),
+                                          N.ptr(theta_bar), N.ptr(sbar), E._stream()))
+    return sbar
+
+
+def batch_cf(tape: BatchTape, n2: np.ndarray, e0: np.ndarray, sign: int, zt: torch.Tensor, g: torch.Tensor) -> None:
+    """g[b] += the continued fraction of tape b (norm^2 n2[b], shift e0[b]), every problem in
+    one launch."""
+    B, dev = len(tape.m), E.device()
+    m_d = torch.tensor(tape.m, dtype=torch.int32, device=dev)
+    n2_d = torch.as_tensor(np.asarray(n2, dtype=np.float64)).to(dev)
+    e0_d = torch.as_tensor(np.asarray(e0, dtype=np.float64)).to(dev)
+    N.check(N.lib().ed_batch_cf(B, N.ptr(tape.alpha), tape.K, N.ptr(tape.beta), tape.K + 1, N.ptr(m_d), N.ptr(n2_d),
+                                N.ptr(e0_d), int(sign), N.ptr(torch.view_as_real(zt)), zt.numel(),
+                                N.ptr(torch.view_as_real(g)), E._stream()))
+
+
+def batch_cf_adjoint(tape: BatchTape, n2: np.ndarray, e0: np.ndarray, sign: int, zt: torch.Tensor,
+                     gbar: torch.Tensor):
+    """cf_adjoint of every tape of the batch: (abar[B, K], bbar[B, K+1], e0bar[B])."""
+    B, dev = len(tape.m), E.device()
+    abar = torch.zeros((B, tape.K), dtype=torch.float64, device=dev)
+    bbar = torch.zeros((B, tape.K + 1), dtype=torch.float64, device=dev)
+    scal = torch.zeros((B, 2), dtype=torch.float64, device=dev)
+    mmax = max(tape.m) if tape.m else 0
+    if mmax == 0:
+        return abar, bbar, scal[:, 0]
+    m_d = torch.tensor(tape.m, dtype=torch.int32, device=dev)
+    n2_d = torch.as_tensor(np.asarray(n2, dtype=np.float64)).to(dev)
+    e0_d = torch.as_tensor(np.asarray(e0, dtype=np.float64)).to(dev)
+    gb = gbar.to(dtype=torch.complex128).contiguous()
+    N.check(N.lib().ed_batch_cf_adjoint(B, N.ptr(tape.alpha), tape.K, N.ptr(tape.beta), tape.K + 1, N.ptr(m_d), mmax,
+                                        N.ptr(n2_d), N.ptr(e0_d), int(sign), N.ptr(torch.view_as_real(zt)), zt.numel(),
+                                        N.ptr(torch.view_as_real(gb)), N.ptr(abar), N.ptr(bbar), N.ptr(scal),
+                                        E._stream()))
+    return abar, bbar, scal[:, 0]
+
+
+def _apply_fermion_rows(src: E.Plan, dst: E.Plan, pos: int, sigma: int, create: bool, X: torch.Tensor) -> torch.Tensor:
+    """c^dag (create) or c applied to every row of X [B, D_src] -> [B, D_dst]."""
+    B = X.shape[0]
+    Y = torch.empty((B, dst.dim), dtype=torch.float64, device=E.device())
+    N.check(N.lib().ed_apply_fermion(src.handle, dst.handle, int(pos), int(sigma), int(bool(create)), 0,
+                                     N.ptr(X.contiguous()), N.ptr(Y), B, src.dim, dst.dim, E._stream()))
+    return Y
+
+
+def _gf_forward_batch(thetas: torch.Tensor, spec, zt: torch.Tensor, g: torch.Tensor):
+    n_sites, bonds, width, (nu, nd), pos, sigma, m0, mgf, c, seed = spec
+    B = thetas.shape[0]
+    th = thetas.detach().to(dtype=torch.float64).contiguous()
+    dev = E.device()
+    plan = structure_plan(n_sites, bonds, width, nu, nd)
+    diag = batch_diag(plan, th)
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    v0 = torch.rand(plan.dim, generator=gen, dtype=torch.float64).to(dev)
+    tape0 = batch_tape_forward(plan, th, diag, v0.expand(B, -1), m0, c, tol=1e-12)
+    a_h = tape0.alpha.cpu().numpy()
+    b_h = tape0.beta.cpu().numpy()
+    e0 = np.zeros(B)
+    cv = np.zeros((B, tape0.K))
+    for b in range(B):
+        m = tape0.m[b]
+        e0[b], cv[b, :m] = _tridiag_lowest_host(a_h[b, :m], b_h[b, :m + 1])
+    cvec = torch.as_tensor(cv).to(dev)
+    Y, _ = batch_tape_combine(tape0, coef=cvec)
+    ynorm = torch.linalg.norm(Y, dim=1)
+    psi = Y / ynorm[:, None]
+    parts = []
+    for delta, create, sign in ((1, True, 1), (-1, False, -1)):
+        tu, td = (nu + delta, nd) if sigma == 1 else (nu, nd + delta)
+        if not (0 <= tu <= n_sites and 0 <= td <= n_sites):
+            parts.append(None)
+            continue
+        tp = structure_plan(n_sites, bonds, width, tu, td)
+        start = _apply_fermion_rows(plan, tp, pos, sigma, create, psi)
+        tape = batch_tape_forward(tp, th, batch_diag(tp, th), start, mgf, c)
+        n2 = tape.beta[:, 0].cpu().numpy() ** 2
+        batch_cf(tape, n2, e0, sign, zt, g)
+        parts.append((tp, tape, sign, create, n2))
+    return (plan, tape0, a_h, b_h, cv, e0, ynorm, psi, zt, parts, spec)
+
+
+def _gf_backward_batch(saved, gbar: torch.Tensor) -> torch.Tensor:
+    plan, tape0, a_h, b_h, cv, e0, ynorm, psi, zt, parts, spec = saved
+    n_sites, bonds = spec[0], spec[1]
+    B = psi.shape[0]
+    dev = E.device()
+    P = 2 * n_sites + len(bonds)
+    theta_bar = torch.zeros((B, P), dtype=torch.float64, device=dev)
+    e0bar = torch.zeros(B, dtype=torch.float64, device=dev)
+    psibar = torch.zeros_like(psi)
+    gb = gbar.to(dev).contiguous()
+    pos, sigma = spec[4], spec[5]
+    for part in parts:
+        if part is None:
+            continue
+        tp, tape, sign, create, n2 = part
+        Ab, Bb, eb = batch_cf_adjoint(tape, n2, e0, sign, zt, gb)
+        e0bar += eb
+        sbar = batch_tape_reverse(tape, Ab, Bb, theta_bar)
+        psibar = psibar + _apply_fermion_rows(tp, plan, pos, sigma, not create, sbar)
+    ybar = (psibar - torch.sum(psibar * psi, dim=1, keepdim=True) * psi) / ynorm[:, None]
+    _, cbar_d = batch_tape_combine(tape0, probe=ybar)
+    cbar = cbar_d.cpu().numpy()
+    eb_h = e0bar.cpu().numpy()
+    # v_b = -(T_b - E0_b)^+ cbar_b for every problem in one stacked solve: each system is
+    # padded to the longest tape with identity rows (zero right-hand side there)
+    mm = max(tape0.m)
+    Ms = np.zeros((B, mm, mm))
+    rhs = np.zeros((B, mm))
+    for b in range(B):
+        m = tape0.m[b]
+        cvec = cv[b, :m]
+        Ms[b, :m, :m] = (np.diag(a_h[b, :m] - e0[b]) + np.diag(b_h[b, 1:m], 1) + np.diag(b_h[b, 1:m], -1)
+                         + np.outer(cvec, cvec))
+        Ms[b, m:, m:] = np.eye(mm - m)
+        rhs[b, :m] = cbar[b, :m] - np.dot(cbar[b, :m], cvec) * cvec
+    vs = -np.linalg.solve(Ms, rhs[..., None])[..., 0]
+    A0 = np.zeros((B, tape0.K))
+    B0 = np.zeros((B, tape0.K + 1))
+    for b in range(B):
+        m = tape0.m[b]
+        cvec = cv[b, :m]
+        v = vs[b, :m] - np.dot(vs[b, :m], cvec) * cvec
+        A0[b, :m] = eb_h[b] * cvec ** 2 + v * cvec
+        if m > 1:
+            B0[b, 1:m] = 2.0 * eb_h[b] * cvec[:-1] * cvec[1:] + v[:-1] * cvec[1:] + v[1:] * cvec[:-1]
+    batch_tape_reverse(tape0, torch.as_tensor(A0).to(dev), torch.as_tensor(B0).to(dev), theta_bar,
+                       ext_coef=torch.as_tensor(cv).to(dev), ext_vec=ybar)
+    return theta_bar
 
 
 class GreensFunctionADBatch(torch.autograd.Function):
-    """G(z) of B problems with the same structure (rows of theta), forward and backward spread
-    over worker threads and streams."""
+    """G(z) of B problems with the same structure (rows of theta), every Lanczos step of all
+    problems in one launch per kernel."""
 
     @staticmethod
-    def forward(ctx, thetas, spec, z, workers):
+    def forward(ctx, thetas, spec, z):
         zt = E._as_dev_c128(z)
-        B = thetas.shape[0]
-        g = torch.zeros((B, zt.numel()), dtype=torch.complex128, device=E.device())
-        saved = [None] * B
-
-        def fwd(i):
-            saved[i] = _gf_forward(thetas[i], spec, zt, g[i])
-
-        _on_workers(B, workers, fwd)
-        ctx.saved = saved
-        ctx.workers = workers
+        g = torch.zeros((thetas.shape[0], zt.numel()), dtype=torch.complex128, device=E.device())
+        ctx.saved = _gf_forward_batch(thetas, spec, zt, g)
         return g
 
     @staticmethod
     def backward(ctx, gbar):
-        saved = ctx.saved
-        B = len(saved)
-        P = 2 * saved[0][-1][0] + len(saved[0][-1][1])
-        out = torch.zeros((B, P), dtype=torch.float64, device=E.device())
-        gb = gbar.contiguous()
-
-        def bwd(i):
-            out[i].copy_(_gf_backward(saved[i], gb[i]))
-
-        _on_workers(B, ctx.workers, bwd)
-        return out.to(gbar.device), None, None, None
+        return _gf_backward_batch(ctx.saved, gbar).to(gbar.device), None, None
 
 
 def greens_function_ad(theta: torch.Tensor, n_sites: int, bonds, sector, z, pos: int = 0, sigma: int = 1,
@@ -327,15 +511,17 @@ def greens_function_ad(theta: torch.Tensor, n_sites: int, bonds, sector, z, pos:
 
 def greens_function_ad_batch(thetas: torch.Tensor, n_sites: int, bonds, sector, z, pos: int = 0, sigma: int = 1,
                              sign_width: int | None = None, gs_steps: int = 200, gf_levels: int = 200,
-                             ckpt: int = 16, seed: int = 0, workers: int = 8) -> torch.Tensor:
+                             ckpt: int = 16, seed: int = 0) -> torch.Tensor:
     """Differentiable T=0 G(z) of B models with one structure (thetas[B, P], rows as in
-    greens_function_ad) -> [B, n_z]. Each problem's arithmetic is that of greens_function_ad;
-    the problems run concurrently on `workers` CUDA streams."""
+    greens_function_ad) -> [B, n_z]. Each problem follows the arithmetic of greens_function_ad;
+    every Lanczos step of all B problems runs as one launch per kernel (batched tape)."""
     spec = (n_sites, [tuple(b) for b in bonds], n_sites if sign_width is None else sign_width, tuple(sector), pos,
             sigma, gs_steps, gf_levels, ckpt, seed)
     if thetas.dim() != 2:
         raise ValueError("thetas must be [B, P]")
-    return GreensFunctionADBatch.apply(thetas, spec, z, max(1, min(int(workers), thetas.shape[0])))
+    if thetas.shape[1] != 2 * n_sites + len(spec[1]):
+        raise ValueError("thetas must have 2 * n_sites + n_bonds columns")
+    return GreensFunctionADBatch.apply(thetas, spec, z)
 
 
 def siam_parameters(u, eps_imp, eps_bath, v, mu=None):

@@ -9,59 +9,9 @@
 #include <cmath>
 #include <vector>
 
-#include "ed_plan.cuh"
+#include "ed_adjoint.cuh"
 
 namespace ed {
-
-constexpr int SW_SITES = 16;
-constexpr int SW_BONDS = 32;
-constexpr int SW_P = 2 * SW_SITES + SW_BONDS;
-constexpr int SW_NT = 128;
-
-struct SandwichArgs {
-  const uint64_t* up_states; const uint64_t* dn_states;
-  const int32_t* up_off; const int32_t* up_idx; const double* up_coef; const int16_t* up_bond;
-  const int32_t* dn_off; const int32_t* dn_idx; const double* dn_coef; const int16_t* dn_bond;
-  int64_t nu, nd;
-};
-
-// Row i's terms of a^T (dH/dtheta) b, added to the calling thread's accumulator column
-// acc[p * SW_NT] (p in the packed order [eps(ns), U(ns), t(nb)]; the column lives in shared
-// memory, so a term costs one add whatever the parameter count). bi = b[i].
-__device__ __forceinline__ void sandwich_row(const SandwichArgs& g, int ns, int64_t i, double ai, double bi,
-                                             const double* __restrict__ b, double* acc) {
-  const int64_t u = i / g.nd, d = i - u * g.nd;
-  const double pr = ai * bi;
-  const uint64_t su = g.up_states[u], sd = g.dn_states[d];
-  for (uint64_t bits = su; bits; bits &= bits - 1) acc[(__ffsll((long long)bits) - 1) * SW_NT] += pr;
-  for (uint64_t bits = sd; bits; bits &= bits - 1) acc[(__ffsll((long long)bits) - 1) * SW_NT] += pr;
-  for (uint64_t bits = su & sd; bits; bits &= bits - 1) acc[(ns + __ffsll((long long)bits) - 1) * SW_NT] += pr;
-  const int32_t u0 = g.up_off[u], u1 = g.up_off[u + 1];
-  for (int32_t e = u0; e < u1; ++e)
-    acc[(2 * ns + g.up_bond[e]) * SW_NT] += ai * copysign(1.0, g.up_coef[e]) * b[(int64_t)g.up_idx[e] * g.nd + d];
-  const int32_t d0 = g.dn_off[d], d1 = g.dn_off[d + 1];
-  for (int32_t e = d0; e < d1; ++e)
-    acc[(2 * ns + g.dn_bond[e]) * SW_NT] += ai * copysign(1.0, g.dn_coef[e]) * b[u * g.nd + g.dn_idx[e]];
-}
-
-__device__ __forceinline__ void sandwich_zero(double* sacc, int P) {
-  for (int t = threadIdx.x; t < P * SW_NT; t += SW_NT) sacc[t] = 0.0;
-  __syncthreads();
-}
-
-// the block's P sums (threads in a fixed order) into out_row[0..P), written or added
-__device__ __forceinline__ void sandwich_block_out(const double* sacc, int P, double* out_row, bool accumulate) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  __syncthreads();
-  for (int p = warp; p < P; p += SW_NT / 32) {
-    double v = 0.0;
-#pragma unroll
-    for (int r = 0; r < SW_NT / 32; ++r) v += sacc[p * SW_NT + lane + 32 * r];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) out_row[p] = accumulate ? out_row[p] + v : v;
-  }
-}
 
 __global__ void __launch_bounds__(SW_NT) k_sandwich(SandwichArgs g, int ns, int P, const double* __restrict__ a,
                                                     const double* __restrict__ b, double* __restrict__ partial) {
@@ -83,7 +33,6 @@ __global__ void k_param_reduce(const double* __restrict__ partial, int nblocks, 
   out[p] = accumulate ? out[p] + s : s;
 }
 
-static size_t sandwich_smem(int P) { return (size_t)P * SW_NT * sizeof(double); }
 
 // ---- taped FP64 Lanczos, segment recompute and reverse sweep --------------------------------
 // The forward is the plain three-term recurrence (no reorthogonalisation) of the reference's
@@ -95,8 +44,6 @@ static size_t sandwich_smem(int P) { return (size_t)P * SW_NT * sizeof(double); 
 // recomputed q_k equals the forward's bit for bit. The reverse sweep is the exact adjoint of
 // those recurrences; the parameter gradient term w_bar^T (dH/dtheta) q_k of each step is fused
 // into the step's elementwise kernel and accumulated per block across steps.
-constexpr int TP_NT = 256;
-
 struct TapeState {
   int stop;   // 0 running, 1 converged, 2 breakdown (invariant subspace)
   int steps;  // m once stopped
@@ -105,23 +52,6 @@ struct TapeState {
 };
 
 __device__ __forceinline__ bool tp_stopped(const int* stop) { return stop && *(volatile const int*)stop != 0; }
-
-__device__ __forceinline__ bool tp_last_block(unsigned int* ticket) {
-  __shared__ bool am_last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (am_last) __threadfence();
-  return am_last;
-}
-
-// sum of row j of partial[j * nb + b] over b in block order (whole block; valid in thread 0)
-__device__ __forceinline__ double tp_row_sum(const double* partial, int nb, double* sm) {
-  double v = 0.0;
-  for (int b = threadIdx.x; b < nb; b += TP_NT) v += ((volatile const double*)partial)[b];
-  return block_sum<TP_NT>(v, sm);
-}
 
 // *res = <a, b> (and sqrt -> *res_sqrt)
 __global__ void __launch_bounds__(TP_NT) k_tp_dot(const double* __restrict__ a, const double* __restrict__ b,
@@ -151,13 +81,6 @@ __global__ void k_tp_scale(const double* __restrict__ v, double* __restrict__ ou
   const double s = 1.0 / *scale;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     out[i] = v[i] * s;
-}
-
-// the residual of step k, element i (shared by the forward and the recompute)
-__device__ __forceinline__ double tp_resid(double w, double a, double q, double b, const double* qp, int64_t i) {
-  double x = fma(-a, q, w);
-  if (qp) x = fma(-b, qp[i], x);
-  return x;
 }
 
 // w <- w - alpha_k q_k - beta_k q_{k-1}; beta_{k+1} = ||w||; breakdown when
@@ -347,107 +270,6 @@ __global__ void k_tp_startbar(const double* __restrict__ qb0, const double* __re
     out[i] = fma(b0, q0[i], (qb0[i] - d * q0[i]) * ib);
 }
 
-// ---- continued fraction adjoint ------------------------------------------------------------
-// G(z) = sign n2 / t_0, t_l = z' - alpha_l - beta_{l+1}^2 / t_{l+1}, t_{m-1} = z' - alpha_{m-1},
-// z' = sign z + shift. For L = Re sum_z conj(gbar_z) G_z the adjoints follow the chain
-// u_0 = dG/dt_0 = -sign n2 / t_0^2, u_{l+1} = u_l beta_{l+1}^2 / t_{l+1}^2:
-//   dG/dalpha_l = -u_l, dG/dbeta_{l+1} = -2 u_l beta_{l+1} / t_{l+1}, dG/dshift = sum_l u_l,
-//   dG/dn2 = sign / t_0.
-// One thread per frequency; per-level block sums to partial rows [2m + 2][G], the last block
-// sums them in block order.
-constexpr int CFA_NT = 256;
-
-__device__ __forceinline__ double2 c_mul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ double2 c_div(double2 a, double2 b) {
-  const double d = b.x * b.x + b.y * b.y;
-  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
-}
-
-__global__ void __launch_bounds__(CFA_NT) k_cf_adjoint(const double* __restrict__ a, const double* __restrict__ b,
-                                                       int m, double n2, double shift, int sign,
-                                                       const double2* __restrict__ z, int64_t nz,
-                                                       const double2* __restrict__ gbar, double2* __restrict__ ts,
-                                                       double* partial, unsigned int* ticket, double* abar,
-                                                       double* bbar, double* scal) {
-  __shared__ double sm[CFA_NT / 32];
-  const int G = gridDim.x;
-  const int64_t i = blockIdx.x * (int64_t)CFA_NT + threadIdx.x;
-  const bool ok = i < nz;
-  double2 cg = make_double2(0.0, 0.0), zp = make_double2(0.0, 0.0);
-  if (ok) {
-    cg = make_double2(gbar[i].x, -gbar[i].y);
-    zp = make_double2(sign * z[i].x + shift, sign * z[i].y);
-    double2 t = make_double2(zp.x - a[m - 1], zp.y);
-    ts[(int64_t)(m - 1) * nz + i] = t;
-    for (int l = m - 2; l >= 0; --l) {
-      const double bb = b[l + 1] * b[l + 1];
-      const double2 q = c_div(make_double2(bb, 0.0), t);
-      t = make_double2(zp.x - a[l] - q.x, zp.y - q.y);
-      ts[(int64_t)l * nz + i] = t;
-    }
-  }
-  double2 t0 = ok ? ts[i] : make_double2(1.0, 0.0);
-  double2 u = ok ? c_div(make_double2(-sign * n2, 0.0), c_mul(t0, t0)) : make_double2(0.0, 0.0);
-  double2 dz = make_double2(0.0, 0.0);
-  for (int l = 0; l < m; ++l) {
-    dz.x += u.x;
-    dz.y += u.y;
-    const double ca = -(cg.x * u.x - cg.y * u.y);  // Re(cg * (-u))
-    double cb = 0.0;
-    double2 t1 = make_double2(1.0, 0.0);
-    if (l + 1 < m && ok) {
-      t1 = ts[(int64_t)(l + 1) * nz + i];
-      const double2 f = c_div(make_double2(-2.0 * b[l + 1], 0.0), t1);
-      const double2 uf = c_mul(u, f);
-      cb = cg.x * uf.x - cg.y * uf.y;
-    }
-    const double sa = block_sum<CFA_NT>(ok ? ca : 0.0, sm);
-    const double sb = block_sum<CFA_NT>(cb, sm);
-    if (threadIdx.x == 0) {
-      partial[(int64_t)l * G + blockIdx.x] = sa;
-      partial[(int64_t)(m + l) * G + blockIdx.x] = sb;
-    }
-    if (l + 1 < m && ok) {
-      const double bb = b[l + 1] * b[l + 1];
-      u = c_mul(u, c_div(make_double2(bb, 0.0), c_mul(t1, t1)));
-    }
-  }
-  const double ce = ok ? cg.x * dz.x - cg.y * dz.y : 0.0;
-  double cn = 0.0;
-  if (ok) {
-    const double2 f = c_div(make_double2((double)sign, 0.0), t0);
-    cn = cg.x * f.x - cg.y * f.y;
-  }
-  const double se = block_sum<CFA_NT>(ce, sm);
-  const double sn = block_sum<CFA_NT>(cn, sm);
-  if (threadIdx.x == 0) {
-    partial[(int64_t)(2 * m) * G + blockIdx.x] = se;
-    partial[(int64_t)(2 * m + 1) * G + blockIdx.x] = sn;
-  }
-  __shared__ bool am_last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (!am_last) return;
-  __threadfence();
-  // one row per thread, blocks summed in order
-  for (int r = threadIdx.x; r < 2 * m + 2; r += CFA_NT) {
-    double t = 0.0;
-    for (int bk = 0; bk < G; ++bk) t += ((volatile const double*)partial)[(int64_t)r * G + bk];
-    if (r < m) abar[r] = t;
-    else if (r < 2 * m) { if (r - m + 1 < m) bbar[r - m + 1] = t; }
-    else if (r == 2 * m) scal[0] = t;
-    else { scal[1] = t; bbar[0] = 2.0 * sqrt(n2) * t; }
-  }
-  if (threadIdx.x == 0) {
-    bbar[m] = 0.0;
-    *ticket = 0;
-  }
-}
-
 }  // namespace ed
 
 using namespace ed;
@@ -478,8 +300,7 @@ ED_API ed_status ed_param_sandwich(ed_plan p, const double* d_a, const double* d
   const int nb = (int)std::max<int64_t>(1, std::min<int64_t>((p->dim + SW_NT - 1) / SW_NT, (int64_t)p->ctx->num_sms * 2));
   double* partial = nullptr;
   ED_CUDA(cudaMallocAsync(&partial, (size_t)nb * SW_P * sizeof(double), s));
-  SandwichArgs g{p->up.states, p->dn.states, p->up.off, p->up.idx, p->up.coef, p->up.bond,
-                 p->dn.off, p->dn.idx, p->dn.coef, p->dn.bond, p->num_up, p->num_dn};
+  const SandwichArgs g = sandwich_args(p);
   const int P = 2 * p->n_sites + (int)p->hop.size();
   ED_TRY(sandwich_attrs());
   k_sandwich<<<nb, SW_NT, sandwich_smem(P), s>>>(g, p->n_sites, P, d_a, d_b, partial);
@@ -516,80 +337,6 @@ TapeLayout tape_layout(const ed_plan_s* p, int K, int c) {
   L.off_state = o; o = tp_align(o + sizeof(TapeState));
   L.total = o;
   return L;
-}
-
-// Lowest eigenpair of the tridiagonal (a[0..m), b[1..m)) on the host, FP64: bisection on the
-// Sturm count of the LDL^T pivots, then two steps of inverse iteration (Gaussian elimination
-// with partial pivoting). Used by the taped Lanczos' convergence test, which reads the scalars
-// at its synchronisation points anyway; a one-thread FP64 solve is far slower on the device.
-double host_tridiag_lowest(const double* a, const double* b, int m, std::vector<double>& c) {
-  double lo = a[0], hi = a[0];
-  for (int i = 0; i < m; ++i) {
-    const double r = (i > 0 ? std::fabs(b[i]) : 0.0) + (i + 1 < m ? std::fabs(b[i + 1]) : 0.0);
-    lo = std::min(lo, a[i] - r);
-    hi = std::max(hi, a[i] + r);
-  }
-  const double pad = 1e-12 * std::max(std::fabs(lo), std::fabs(hi)) + 1e-300;
-  lo -= pad;
-  hi += pad;
-  auto count = [&](double x) {
-    int n = 0;
-    double q = a[0] - x;
-    for (int i = 0;;) {
-      if (q == 0.0) q = -1e-300;
-      if (q < 0.0) ++n;
-      if (++i >= m) break;
-      q = (a[i] - x) - b[i] * b[i] / q;
-    }
-    return n;
-  };
-  for (int it = 0; it < 200 && hi - lo > 4e-16 * std::max(std::fabs(lo), std::fabs(hi)) + 1e-300; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (count(mid) >= 1) hi = mid; else lo = mid;
-  }
-  const double ev = 0.5 * (lo + hi);
-  c.assign(m, 1.0 / std::sqrt((double)m));
-  for (int i = 0; i < m; ++i) c[i] *= 1.0 + 0.01 * (double)((i * 7919) % 13) / 13.0;
-  std::vector<double> dd(m), du(m), du2(m), ml(m);
-  std::vector<char> pv(m);
-  const double tiny = 1e-300 + 1e-18 * std::max(std::fabs(ev), 1.0);
-  for (int it = 0; it < 2; ++it) {
-    for (int i = 0; i < m; ++i) { dd[i] = a[i] - ev; du[i] = (i + 1 < m) ? b[i + 1] : 0.0; du2[i] = 0.0; }
-    for (int i = 0; i + 1 < m; ++i) {
-      const double sub = b[i + 1];
-      if (std::fabs(dd[i]) >= std::fabs(sub)) {
-        pv[i] = 0;
-        if (dd[i] == 0.0) dd[i] = tiny;
-        ml[i] = sub / dd[i];
-        dd[i + 1] -= ml[i] * du[i];
-      } else {
-        pv[i] = 1;
-        const double l = dd[i] / sub, t0 = dd[i + 1], t1 = (i + 2 < m) ? du[i + 1] : 0.0, odu = du[i];
-        ml[i] = l;
-        dd[i] = sub;
-        du[i] = t0;
-        du2[i] = t1;
-        dd[i + 1] = odu - l * t0;
-        if (i + 2 < m) du[i + 1] = -l * t1;
-      }
-    }
-    if (dd[m - 1] == 0.0) dd[m - 1] = tiny;
-    for (int i = 0; i + 1 < m; ++i) {
-      if (pv[i]) { const double t = c[i]; c[i] = c[i + 1]; c[i + 1] = t - ml[i] * c[i]; }
-      else c[i + 1] -= ml[i] * c[i];
-    }
-    for (int i = m - 1; i >= 0; --i) {
-      double s = c[i];
-      if (i + 1 < m) s -= du[i] * c[i + 1];
-      if (i + 2 < m) s -= du2[i] * c[i + 2];
-      c[i] = s / dd[i];
-    }
-    double nrm = 0.0;
-    for (int i = 0; i < m; ++i) nrm += c[i] * c[i];
-    nrm = 1.0 / std::sqrt(nrm);
-    for (int i = 0; i < m; ++i) c[i] *= nrm;
-  }
-  return ev;
 }
 
 ed_status tape_check(const ed_plan_s* p, int K, int c) {
@@ -761,8 +508,7 @@ ED_API ed_status ed_tape_reverse(ed_plan p, int m, int ckpt, const double* d_alp
   ED_CUDA(cudaMemsetAsync(psw, 0, (size_t)L.nsw * SW_P * sizeof(double), s));
   ED_CUDA(cudaMemcpyAsync(AB, d_abar, m * sizeof(double), cudaMemcpyDeviceToDevice, s));
   ED_CUDA(cudaMemcpyAsync(BB, d_bbar, (m + 1) * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  SandwichArgs g{p->up.states, p->dn.states, p->up.off, p->up.idx, p->up.coef, p->up.bond,
-                 p->dn.off, p->dn.idx, p->dn.coef, p->dn.bond, p->num_up, p->num_dn};
+  const SandwichArgs g = sandwich_args(p);
   const int gv = L.nparts;
   const int P = 2 * p->n_sites + (int)p->hop.size();
   ED_TRY(sandwich_attrs());
@@ -821,20 +567,8 @@ ED_API ed_status ed_cf_adjoint(const double* d_alpha, const double* d_beta, int 
   if (sign != 1 && sign != -1) return fail(ED_ERR_INVALID_ARG, "sign must be +1 or -1");
   if (!d_alpha || !d_beta || !d_z || !d_gbar || !d_abar || !d_bbar || !d_scal)
     return fail(ED_ERR_INVALID_ARG, "null argument");
-  cudaStream_t s = as_stream(stream);
-  const int G = (int)((n_z + CFA_NT - 1) / CFA_NT);
-  const size_t ts_bytes = (size_t)m * n_z * sizeof(double2);
-  const size_t part_bytes = (size_t)(2 * m + 2) * G * sizeof(double);
-  char* buf = nullptr;
-  ED_CUDA(cudaMallocAsync((void**)&buf, ts_bytes + part_bytes + 256, s));
-  unsigned int* ticket = (unsigned int*)(buf + ts_bytes + part_bytes);
-  ED_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));
-  k_cf_adjoint<<<G, CFA_NT, 0, s>>>(d_alpha, d_beta, m, norm2, shift, sign, (const double2*)d_z, n_z,
-                                    (const double2*)d_gbar, (double2*)buf, (double*)(buf + ts_bytes), ticket, d_abar,
-                                    d_bbar, d_scal);
-  ED_CHECK_LAUNCH("k_cf_adjoint");
-  ED_CUDA(cudaFreeAsync(buf, s));
-  return ED_OK;
+  CfaBatch cb{d_alpha, m, d_beta, m + 1, nullptr, nullptr, nullptr, m, norm2, shift, sign, d_gbar, d_abar, d_bbar, d_scal};
+  return cf_adjoint_launch(cb, 1, m, (const double2*)d_z, n_z, as_stream(stream));
 }
 
 }  // extern "C"

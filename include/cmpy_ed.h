@@ -346,6 +346,55 @@ ED_API ed_status ed_tape_reverse(ed_plan plan, int m, int ckpt, const double* d_
                                  const double* d_bbar, const double* d_ext_coef,
                                  const double* d_ext_vec, void* d_work, size_t work_bytes,
                                  double* d_theta_bar, double* d_start_bar, ed_stream_t stream);
+/* Batched tape: B problems sharing one structure plan (the sector and bonds of `plan`, which
+ * is built with t = 1 on every bond, so its coefficients are the fermionic signs; its eps and
+ * U are unused) with per-problem parameters d_theta[B][P] (layout of ed_plan_num_params).
+ * Vectors are problem-major [B][D]; alpha is [B][max_steps], beta [B][max_steps+1], the
+ * checkpoints [slot][2][B][D]. Problem b's arithmetic is that of the single-problem tape;
+ * h_steps / h_m hold the B tape lengths. ed_batch_diag writes the per-problem diagonal
+ * d_diag[B][D] that the others take; ed_batch_matvec_params applies H_b to x[b]. */
+ED_API ed_status ed_batch_diag(ed_plan plan, int B, const double* d_theta, double* d_diag,
+                               ed_stream_t stream);
+ED_API ed_status ed_batch_matvec_params(ed_plan plan, int B, const double* d_theta,
+                                        const double* d_diag, const double* d_x, double* d_y,
+                                        ed_stream_t stream);
+ED_API ed_status ed_batch_tape_workspace(ed_plan plan, int B, int max_steps, int ckpt,
+                                         size_t* bytes);
+ED_API ed_status ed_batch_lanczos_tape(ed_plan plan, int B, const double* d_theta,
+                                       const double* d_diag, const double* d_start, int max_steps,
+                                       int ckpt, double tol, int check_every, double breakdown,
+                                       void* d_work, size_t work_bytes, double* d_alpha,
+                                       double* d_beta, double* d_ckpt, int* h_steps,
+                                       ed_stream_t stream);
+ED_API ed_status ed_batch_tape_combine(ed_plan plan, int B, const double* d_theta,
+                                       const double* d_diag, const int* h_m, int max_steps,
+                                       int ckpt, const double* d_alpha, const double* d_beta,
+                                       const double* d_ckpt, const double* d_coef, double* d_out,
+                                       const double* d_probe, double* d_dots, void* d_work,
+                                       size_t work_bytes, ed_stream_t stream);
+ED_API ed_status ed_batch_tape_reverse(ed_plan plan, int B, const double* d_theta,
+                                       const double* d_diag, const int* h_m, int max_steps,
+                                       int ckpt, const double* d_alpha, const double* d_beta,
+                                       const double* d_ckpt, const double* d_abar,
+                                       const double* d_bbar, const double* d_ext_coef,
+                                       const double* d_ext_vec, void* d_work, size_t work_bytes,
+                                       double* d_theta_bar, double* d_start_bar,
+                                       ed_stream_t stream);
+/* Continued fractions of B tapes at once (the arithmetic of ed_gf_continued_fraction):
+ * d_g[b][j] += sign n2[b] / (z'_j - alpha[b][0] - beta[b][1]^2 / ...), z' = sign z + shift[b],
+ * m[b] levels (problems with m[b] = 0 are skipped); alpha[b][l] = d_alpha[b*ka + l],
+ * beta[b][l] = d_beta[b*kb + l]. ed_batch_cf_adjoint is ed_cf_adjoint per problem
+ * (d_abar[b*ka + l], d_bbar[b*kb + l], d_scal[2b], d_scal[2b+1]); m_max = max m[b]. */
+ED_API ed_status ed_batch_cf(int B, const double* d_alpha, int64_t ka, const double* d_beta,
+                             int64_t kb, const int* d_m, const double* d_n2, const double* d_shift,
+                             int sign, const double* d_z, int64_t n_z, double* d_g,
+                             ed_stream_t stream);
+ED_API ed_status ed_batch_cf_adjoint(int B, const double* d_alpha, int64_t ka,
+                                     const double* d_beta, int64_t kb, const int* d_m, int m_max,
+                                     const double* d_n2, const double* d_shift, int sign,
+                                     const double* d_z, int64_t n_z, const double* d_gbar,
+                                     double* d_abar, double* d_bbar, double* d_scal,
+                                     ed_stream_t stream);
 /* Adjoint of the continued fraction of ed_gf_continued_fraction: for
  * L = Re sum_j conj(gbar_j) G(z_j) (d_z, d_gbar interleaved complex), d_abar[l] = dL/dalpha_l,
  * d_bbar[l] = dL/dbeta_l (l = 1..m-1; d_bbar[0] = dL/d sqrt(norm2), d_bbar[m] = 0),

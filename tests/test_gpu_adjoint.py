@@ -144,8 +144,9 @@ def test_adjoint_checkpoint_invariance(cuda):
 
 
 def test_adjoint_batch_equals_single(cuda):
-    """greens_function_ad_batch (problems on several streams and host threads) gives each
-    problem exactly the forward and gradient of greens_function_ad."""
+    """greens_function_ad_batch (all problems in each launch) gives each problem the forward
+    and the gradient of greens_function_ad (same arithmetic; the reductions are blocked
+    differently, so to rounding)."""
     from cmpy_gb300.adjoint import greens_function_ad, greens_function_ad_batch
 
     rng = np.random.default_rng(41)
@@ -163,7 +164,7 @@ def test_adjoint_batch_equals_single(cuda):
         th, n_sites, bonds, width = _siam_theta(4.0, eb[i], v[i])
         rows.append(th)
     thetas = torch.stack(rows)
-    g = greens_function_ad_batch(thetas, n_sites, bonds, (2, 3), z, sign_width=width, workers=3, **kw)
+    g = greens_function_ad_batch(thetas, n_sites, bonds, (2, 3), z, sign_width=width, **kw)
     _loss(g, gt.expand_as(g)).backward()
 
     for i in range(B):
@@ -171,7 +172,7 @@ def test_adjoint_batch_equals_single(cuda):
         vi = torch.tensor(v0[i], dtype=torch.float64, device="cuda", requires_grad=True)
         th, _, _, _ = _siam_theta(4.0, ebi, vi)
         gi = greens_function_ad(th, n_sites, bonds, (2, 3), z, sign_width=width, **kw)
-        assert torch.equal(gi.detach(), g[i].detach())
+        torch.testing.assert_close(gi.detach(), g[i].detach(), rtol=1e-10, atol=1e-12)
         _loss(gi, gt).backward()
-        assert torch.equal(ebi.grad, eb.grad[i])
-        assert torch.equal(vi.grad, v.grad[i])
+        torch.testing.assert_close(ebi.grad, eb.grad[i], rtol=1e-8, atol=1e-10)
+        torch.testing.assert_close(vi.grad, v.grad[i], rtol=1e-8, atol=1e-10)

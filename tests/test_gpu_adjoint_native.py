@@ -170,3 +170,112 @@ def test_cf_adjoint_matches_torch(cuda, sign):
     torch.testing.assert_close(abar, abar_r, rtol=1e-11, atol=1e-13)
     torch.testing.assert_close(bbar, bbar_r, rtol=1e-11, atol=1e-13)
     assert abs(e0bar.item() - e0bar_r.item()) < 1e-11 * max(1.0, abs(e0bar_r.item()))
+
+
+def _batch_thetas(B, nbath, seed):
+    from cmpy_gb300.adjoint import siam_parameters
+
+    rng = np.random.default_rng(seed)
+    rows = []
+    for _ in range(B):
+        eb = torch.tensor(rng.uniform(-2, 2, nbath), dtype=torch.float64, device="cuda")
+        v = torch.tensor(rng.uniform(0.1, 0.6, nbath), dtype=torch.float64, device="cuda")
+        th, n_sites, bonds, width = siam_parameters(torch.tensor(4.0, dtype=torch.float64, device="cuda"),
+                                                    torch.tensor(0.0, dtype=torch.float64, device="cuda"), eb, v)
+        rows.append(th)
+    return torch.stack(rows).contiguous(), n_sites, bonds, width
+
+
+def test_batch_matvec_bit_identical_to_single(cuda):
+    """H(theta_b) x_b of the batched kernel equals each problem's own plan matvec bit for bit."""
+    from cmpy_gb300.adjoint import batch_diag, batch_matvec, plan_from_params, structure_plan
+
+    thetas, n_sites, bonds, width = _batch_thetas(4, 5, 31)
+    sp = structure_plan(n_sites, bonds, width, 3, 3)
+    diag = batch_diag(sp, thetas)
+    X = torch.rand((4, sp.dim), dtype=torch.float64, device="cuda") - 0.5
+    Y = batch_matvec(sp, thetas, diag, X)
+    for b in range(4):
+        p = plan_from_params(thetas[b], n_sites, bonds, width, 3, 3)
+        assert torch.equal(Y[b], p.matvec(X[b]))
+
+
+def test_batch_tape_matches_single(cuda):
+    from cmpy_gb300.adjoint import (batch_diag, batch_tape_combine, batch_tape_forward, batch_tape_reverse,
+                                    plan_from_params, structure_plan, tape_combine, tape_forward, tape_reverse)
+
+    B, c = 3, 5
+    thetas, n_sites, bonds, width = _batch_thetas(B, 5, 32)
+    P = thetas.shape[1]
+    sp = structure_plan(n_sites, bonds, width, 3, 3)
+    diag = batch_diag(sp, thetas)
+    starts = torch.stack([_start(sp.dim, 40 + b) for b in range(B)])
+    bt = batch_tape_forward(sp, thetas, diag, starts, 25, c)
+    rng = np.random.default_rng(33)
+    coef = torch.tensor(rng.standard_normal((B, bt.K)), dtype=torch.float64, device="cuda")
+    probe = torch.rand((B, sp.dim), dtype=torch.float64, device="cuda")
+    Yb, Db = batch_tape_combine(bt, coef=coef, probe=probe)
+    abar = torch.tensor(rng.standard_normal((B, bt.K)), dtype=torch.float64, device="cuda")
+    bbar = torch.tensor(rng.standard_normal((B, bt.K + 1)), dtype=torch.float64, device="cuda")
+    ec = torch.tensor(rng.standard_normal((B, bt.K)), dtype=torch.float64, device="cuda")
+    ev = torch.rand((B, sp.dim), dtype=torch.float64, device="cuda")
+    thb = torch.zeros((B, P), dtype=torch.float64, device="cuda")
+    sb = batch_tape_reverse(bt, abar, bbar, thb, ext_coef=ec, ext_vec=ev)
+    for b in range(B):
+        p = plan_from_params(thetas[b], n_sites, bonds, width, 3, 3)
+        t = tape_forward(p, starts[b], 25, c)
+        assert bt.m[b] == t.m
+        m = t.m
+        torch.testing.assert_close(bt.alpha[b, :m], t.alpha, rtol=1e-12, atol=1e-13)
+        torch.testing.assert_close(bt.beta[b, :m + 1], t.beta, rtol=1e-12, atol=1e-13)
+        y, d = tape_combine(t, coef=coef[b, :m], probe=probe[b])
+        torch.testing.assert_close(Yb[b], y, rtol=1e-10, atol=1e-11)
+        torch.testing.assert_close(Db[b, :m], d, rtol=1e-10, atol=1e-11)
+        th = torch.zeros(P, dtype=torch.float64, device="cuda")
+        s1 = tape_reverse(t, abar[b, :m], bbar[b, :m + 1], th, ext_coef=ec[b, :m], ext_vec=ev[b])
+        torch.testing.assert_close(thb[b], th, rtol=1e-8, atol=1e-9 * th.abs().max().item())
+        torch.testing.assert_close(sb[b], s1, rtol=1e-8, atol=1e-9 * s1.abs().max().item())
+
+
+def test_batch_tape_ragged_lengths(cuda):
+    """Problems of one batch stop at different steps (convergence, an eigenvector start that
+    breaks down after one step, a zero start vector); each keeps its own tape length."""
+    from cmpy_gb300.adjoint import batch_diag, batch_tape_forward, plan_from_params, structure_plan, tape_forward
+
+    B = 3
+    thetas, n_sites, bonds, width = _batch_thetas(B, 5, 34)
+    sp = structure_plan(n_sites, bonds, width, 3, 3)
+    diag = batch_diag(sp, thetas)
+    p1 = plan_from_params(thetas[1], n_sites, bonds, width, 3, 3)
+    w, V = torch.linalg.eigh(p1.dense())
+    starts = torch.stack([_start(sp.dim, 50), V[:, 0], torch.zeros(sp.dim, dtype=torch.float64, device="cuda")])
+    bt = batch_tape_forward(sp, thetas, diag, starts, 300, 8, tol=1e-12)
+    assert bt.m[1] == 1 and bt.m[2] == 0
+    assert abs(bt.alpha[1, 0].item() - w[0].item()) < 1e-12 * abs(w[0].item())
+    t0 = tape_forward(plan_from_params(thetas[0], n_sites, bonds, width, 3, 3), starts[0], 300, 8, tol=1e-12)
+    assert bt.m[0] == t0.m < 300
+
+
+def test_batch_continued_fraction_matches_single(cuda):
+    from cmpy_gb300 import engine as E
+    from cmpy_gb300.adjoint import (batch_cf, batch_cf_adjoint, batch_diag, batch_tape_forward, cf_adjoint,
+                                    structure_plan)
+
+    B = 3
+    thetas, n_sites, bonds, width = _batch_thetas(B, 5, 35)
+    sp = structure_plan(n_sites, bonds, width, 3, 3)
+    starts = torch.stack([_start(sp.dim, 60 + b) for b in range(B)])
+    bt = batch_tape_forward(sp, thetas, batch_diag(sp, thetas), starts, 40, 8)
+    zt = torch.as_tensor(1j * (2 * np.arange(100) + 1) * np.pi / 30.0 + 0.05).cuda()
+    n2 = bt.beta[:, 0].cpu().numpy() ** 2
+    e0 = np.array([-3.0, -2.5, -4.0])
+    g = torch.zeros((B, zt.numel()), dtype=torch.complex128, device="cuda")
+    batch_cf(bt, n2, e0, -1, zt, g)
+    gbar = torch.rand((B, zt.numel()), dtype=torch.complex128, device="cuda")
+    Ab, Bb, eb = batch_cf_adjoint(bt, n2, e0, -1, zt, gbar)
+    for b in range(B):
+        m = bt.m[b]
+        gs = E.continued_fraction(bt.alpha[b, :m], bt.beta[b, :m + 1], float(n2[b]), zt, float(e0[b]), -1)
+        assert torch.equal(g[b], gs)
+        ab, bb, e = cf_adjoint(bt.alpha[b, :m], bt.beta[b, :m + 1], float(n2[b]), zt, float(e0[b]), -1, gbar[b])
+        assert torch.equal(Ab[b, :m], ab) and torch.equal(Bb[b, :m + 1], bb) and eb[b].item() == e.item()
