@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(SW_NT) k_tp_rstep(SandwichArgs g, int ns, int 
                                                     double* __restrict__ qbm, double* __restrict__ wbar,
                                                     const double* alpha, const double* beta, const double* abar,
                                                     const double* bbar, int k, int has_next, int first,
-                                                    double* __restrict__ psw) {
+                                                    double* __restrict__ pracc, double* __restrict__ psw) {
   extern __shared__ double sacc[];  // [P][SW_NT]
   sandwich_zero(sacc, P);
   const double ak = alpha[k], ab = abar[k];
@@ -257,8 +257,22 @@ __global__ void __launch_bounds__(SW_NT) k_tp_rstep(SandwichArgs g, int ns, int 
     qbk[i] = fma(ab, w0[i], fma(-ak, rb, first ? 0.0 : qbk[i]));
     if (qbm) qbm[i] = -bk * rb;
     wbar[i] = wb;
-    sandwich_row(g, ns, i, wb, x0, q0, sacc + threadIdx.x);  // w_bar^T (dH/dtheta) q_k, row i
+    // w_bar^T (dH/dtheta) q_k, row i: the hop part now, the diagonal part through sum_k w_bar q_k
+    pracc[i] = fma(wb, x0, first ? 0.0 : pracc[i]);
+    sandwich_hop_terms(g, ns, i, wb, q0, sacc + threadIdx.x);
   }
+  sandwich_block_out(sacc, P, psw + (int64_t)blockIdx.x * SW_P, true);
+}
+
+// the diagonal (eps, U) part of sum_k w_bar_k^T (dH/dtheta) q_k from pracc = sum_k w_bar_k q_k,
+// added to the block rows of psw (same grid as the steps)
+__global__ void __launch_bounds__(SW_NT) k_tp_diag_terms(SandwichArgs g, int ns, int P, const double* __restrict__ pracc,
+                                                         double* __restrict__ psw) {
+  extern __shared__ double sacc[];  // [P][SW_NT]
+  sandwich_zero(sacc, P);
+  const int64_t D = g.nu * g.nd;
+  for (int64_t i = blockIdx.x * (int64_t)SW_NT + threadIdx.x; i < D; i += (int64_t)gridDim.x * SW_NT)
+    sandwich_diag_terms(g, ns, i, pracc[i], sacc + threadIdx.x);
   sandwich_block_out(sacc, P, psw + (int64_t)blockIdx.x * SW_P, true);
 }
 
@@ -279,6 +293,7 @@ using namespace ed;
 static ed_status sandwich_attrs() {
   ED_CUDA(cudaFuncSetAttribute(k_sandwich, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sandwich_smem(SW_P)));
   ED_CUDA(cudaFuncSetAttribute(k_tp_rstep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sandwich_smem(SW_P)));
+  ED_CUDA(cudaFuncSetAttribute(k_tp_diag_terms, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sandwich_smem(SW_P)));
   return ED_OK;
 }
 
@@ -325,7 +340,7 @@ size_t tp_align(size_t x) { return (x + 255) & ~(size_t)255; }
 TapeLayout tape_layout(const ed_plan_s* p, int K, int c) {
   TapeLayout L;
   const int64_t D = p->dim;
-  L.nvec = std::max(4, 2 * c + 5);
+  L.nvec = std::max(4, 2 * c + 6);
   L.nparts = (int)std::max<int64_t>(1, std::min<int64_t>((D + TP_NT - 1) / TP_NT, (int64_t)p->ctx->num_sms * 4));
   L.nsw = (int)std::max<int64_t>(1, std::min<int64_t>((D + SW_NT - 1) / SW_NT, (int64_t)p->ctx->num_sms * 2));
   size_t o = 0;
@@ -497,12 +512,14 @@ ED_API ed_status ed_tape_reverse(ed_plan p, int m, int ckpt, const double* d_alp
   double* BB = AB + m;                          // beta_bar [m+1]
   double* res = BB + (m + 1);                   // q_bar_0 . q_0
   TapeState* st = (TapeState*)(base + L.off_state);
-  // vectors: Qseg [c] (q_{s0+1} .. q_{s1-1}), Wseg [c] (w_{s0} .. w_{s1-1}), q_bar x3, w_bar, tmp
+  // vectors: Qseg [c] (q_{s0+1} .. q_{s1-1}), Wseg [c] (w_{s0} .. w_{s1-1}), q_bar x3, w_bar, tmp,
+  // sum_k w_bar_k q_k
   double* Qs = V;
   double* Ws = V + (int64_t)c * D;
   double* QB = V + (int64_t)2 * c * D;
   double* wbar = QB + 3 * D;
   double* tmp = wbar + D;
+  double* pracc = tmp + D;
   auto qb = [&](int k) -> double* { return QB + (int64_t)(k % 3) * D; };
   ED_CUDA(cudaMemsetAsync(st, 0, sizeof(TapeState), s));
   ED_CUDA(cudaMemsetAsync(psw, 0, (size_t)L.nsw * SW_P * sizeof(double), s));
@@ -543,7 +560,8 @@ ED_API ed_status ed_tape_reverse(ed_plan p, int m, int ckpt, const double* d_alp
       }
       k_tp_rstep<<<L.nsw, SW_NT, sandwich_smem(P), s>>>(g, p->n_sites, P, has_next ? qb(k + 1) : nullptr, has_next ? q(k + 1) : nullptr, q(k),
                                          Ws + (int64_t)(k - s0) * D, qb(k), k > 0 ? qb(k - 1) : nullptr, wbar,
-                                         d_alpha, d_beta, AB, BB, k, has_next ? 1 : 0, k == m - 1 ? 1 : 0, psw);
+                                         d_alpha, d_beta, AB, BB, k, has_next ? 1 : 0, k == m - 1 ? 1 : 0, pracc,
+                                         psw);
       ED_CHECK_LAUNCH("k_tp_rstep");
       ED_TRY(matvec_f64(p, wbar, tmp, 1, D, s, nullptr));
       have_tmp = true;
@@ -554,8 +572,9 @@ ED_API ed_status ed_tape_reverse(ed_plan p, int m, int ckpt, const double* d_alp
   k_tp_radot<<<gv, TP_NT, 0, s>>>(qb(0), tmp, d_ext_vec, d_ext_coef, q0, nullptr,
                                   nullptr, D, d_beta, AB, BB, -1, part, &st->ticket[0], res);
   k_tp_startbar<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(qb(0), q0, D, d_beta, BB, res, d_start_bar);
+  k_tp_diag_terms<<<L.nsw, SW_NT, sandwich_smem(P), s>>>(g, p->n_sites, P, pracc, psw);
   k_param_reduce<<<1, SW_P, 0, s>>>(psw, L.nsw, P, d_theta_bar, 1);
-  ED_CHECK_LAUNCH_N("ed_tape_reverse final", 3);
+  ED_CHECK_LAUNCH_N("ed_tape_reverse final", 4);
   return ED_OK;
 }
 

@@ -26,28 +26,40 @@ struct SandwichArgs {
 
 // Row i's terms of a^T (dH/dtheta) b, added to the calling thread's accumulator column
 // acc[p * SW_NT] (p in the packed order [eps(ns), U(ns), t(nb)]; the column lives in shared
-// memory, so a term costs one add whatever the parameter count). bi = b[i].
-__device__ __forceinline__ void sandwich_row(const SandwichArgs& g, int ns, int64_t i, double ai, double bi,
-                                             const double* __restrict__ b, double* acc) {
+// memory, so a term costs one add whatever the parameter count). The diagonal part (eps, U)
+// depends on a_i b_i only; the hop part gathers b at the row's hop partners.
+__device__ __forceinline__ void sandwich_diag_terms(const SandwichArgs& g, int ns, int64_t i, double pr, double* acc) {
   const int64_t u = i / g.nd, d = i - u * g.nd;
-  const double pr = ai * bi;
   const uint64_t su = g.up_states[u], sd = g.dn_states[d];
   for (uint64_t bits = su; bits; bits &= bits - 1) acc[(__ffsll((long long)bits) - 1) * SW_NT] += pr;
   for (uint64_t bits = sd; bits; bits &= bits - 1) acc[(__ffsll((long long)bits) - 1) * SW_NT] += pr;
   for (uint64_t bits = su & sd; bits; bits &= bits - 1) acc[(ns + __ffsll((long long)bits) - 1) * SW_NT] += pr;
+}
+
+__device__ __forceinline__ void sandwich_hop_terms(const SandwichArgs& g, int ns, int64_t i, double ai,
+                                                   const double* __restrict__ b, double* acc) {
+  const int64_t u = i / g.nd, d = i - u * g.nd;
   // the hop's sign (that of its coefficient) flips the sign bit of a_i: integer operations
   const long long ab = __double_as_longlong(ai);
   const long long sbit = (long long)0x8000000000000000ull;
   const int32_t u0 = g.up_off[u], u1 = g.up_off[u + 1];
   for (int32_t e = u0; e < u1; ++e) {
     const double as = __longlong_as_double(ab ^ (__double_as_longlong(g.up_coef[e]) & sbit));
-    acc[(2 * ns + g.up_bond[e]) * SW_NT] += as * b[(int64_t)g.up_idx[e] * g.nd + d];
+    double* a = acc + (2 * ns + g.up_bond[e]) * SW_NT;
+    *a = fma(as, b[(int64_t)g.up_idx[e] * g.nd + d], *a);
   }
   const int32_t d0 = g.dn_off[d], d1 = g.dn_off[d + 1];
   for (int32_t e = d0; e < d1; ++e) {
     const double as = __longlong_as_double(ab ^ (__double_as_longlong(g.dn_coef[e]) & sbit));
-    acc[(2 * ns + g.dn_bond[e]) * SW_NT] += as * b[u * g.nd + g.dn_idx[e]];
+    double* a = acc + (2 * ns + g.dn_bond[e]) * SW_NT;
+    *a = fma(as, b[u * g.nd + g.dn_idx[e]], *a);
   }
+}
+
+__device__ __forceinline__ void sandwich_row(const SandwichArgs& g, int ns, int64_t i, double ai, double bi,
+                                             const double* __restrict__ b, double* acc) {
+  sandwich_diag_terms(g, ns, i, ai * bi, acc);
+  sandwich_hop_terms(g, ns, i, ai, b, acc);
 }
 
 __device__ __forceinline__ void sandwich_zero(double* sacc, int P) {

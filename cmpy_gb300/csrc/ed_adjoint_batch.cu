@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(SW_NT) k_bt_rstep(SandwichArgs g, int ns, int 
                                                     double* __restrict__ qbm, double* __restrict__ wbar,
                                                     const double* alpha, const double* beta, const double* abar,
                                                     const double* bbar, int K, int k, BState bs,
-                                                    double* __restrict__ psw) {
+                                                    double* __restrict__ pracc, double* __restrict__ psw) {
   const int b = blockIdx.y;
   const int m = bs.m[b];
   if (k >= m) return;
@@ -378,8 +378,23 @@ __global__ void __launch_bounds__(SW_NT) k_bt_rstep(SandwichArgs g, int ns, int 
     qbk[o + i] = fma(ab, w0[o + i], fma(-ak, rb, first ? 0.0 : qbk[o + i]));
     if (qbm) qbm[o + i] = -bk * rb;
     wbar[o + i] = wb;
-    sandwich_row(g, ns, i, wb, x0, q0b, sacc + threadIdx.x);
+    // the hop part now, the diagonal part through sum_k w_bar_k q_k
+    pracc[o + i] = fma(wb, x0, first ? 0.0 : pracc[o + i]);
+    sandwich_hop_terms(g, ns, i, wb, q0b, sacc + threadIdx.x);
   }
+  sandwich_block_out(sacc, P, psw + ((int64_t)b * gridDim.x + blockIdx.x) * SW_P, true);
+}
+
+// the diagonal (eps, U) part from pracc[b] = sum_k w_bar_k q_k (problems with m[b] >= 1)
+__global__ void __launch_bounds__(SW_NT) k_bt_diag_terms(SandwichArgs g, int ns, int P, const double* __restrict__ pracc,
+                                                         BState bs, double* __restrict__ psw) {
+  const int b = blockIdx.y;
+  if (bs.m[b] < 1) return;
+  extern __shared__ double sacc[];  // [P][SW_NT]
+  sandwich_zero(sacc, P);
+  const int64_t D = g.nu * g.nd, o = (int64_t)b * D;
+  for (int64_t i = blockIdx.x * (int64_t)SW_NT + threadIdx.x; i < D; i += (int64_t)gridDim.x * SW_NT)
+    sandwich_diag_terms(g, ns, i, pracc[o + i], sacc + threadIdx.x);
   sandwich_block_out(sacc, P, psw + ((int64_t)b * gridDim.x + blockIdx.x) * SW_P, true);
 }
 
@@ -455,7 +470,7 @@ size_t bt_align(size_t x) { return (x + 255) & ~(size_t)255; }
 BLayout blayout(const ed_plan_s* p, int B, int K, int c) {
   BLayout L;
   const int64_t D = p->dim;
-  L.nvec = std::max(4, 2 * c + 5);
+  L.nvec = std::max(4, 2 * c + 6);
   L.gx = (int)std::max<int64_t>(1, std::min<int64_t>((D + 4 * BT_NT - 1) / (4 * BT_NT), 64));
   L.nsw = (int)std::max<int64_t>(1, std::min<int64_t>((D + 4 * SW_NT - 1) / (4 * SW_NT), 64));
   size_t o = 0;
@@ -712,9 +727,11 @@ ED_API ed_status ed_batch_tape_reverse(ed_plan p, int B, const double* d_theta, 
   double* QB = V + (int64_t)2 * c * BD;
   double* wbar = QB + 3 * BD;
   double* tmp = wbar + BD;
+  double* pracc = tmp + BD;  // [B][D]: sum_k w_bar_k q_k
   auto qb = [&](int k) -> double* { return QB + (int64_t)(k % 3) * BD; };
   const int P = 2 * p->n_sites + (int)p->hop.size();
   ED_CUDA(cudaFuncSetAttribute(k_bt_rstep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sandwich_smem(SW_P)));
+  ED_CUDA(cudaFuncSetAttribute(k_bt_diag_terms, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sandwich_smem(SW_P)));
   ED_CUDA(cudaMemsetAsync(base + L.off_int, 0, (size_t)5 * B * sizeof(int), s));
   ED_CUDA(cudaMemcpyAsync(bs.m, h_m, B * sizeof(int), cudaMemcpyHostToDevice, s));
   ED_CUDA(cudaMemsetAsync(psw, 0, (size_t)B * L.nsw * SW_P * sizeof(double), s));
@@ -751,7 +768,7 @@ ED_API ed_status ed_batch_tape_reverse(ed_plan p, int B, const double* d_theta, 
                                         D, d_beta, AB, BB, K, k, part, bs, nullptr);
         k_bt_rstep<<<gw, SW_NT, sandwich_smem(P), s>>>(g, p->n_sites, P, qb(k + 1), q1, q(k),
                                                       Ws + (int64_t)(k - s0) * BD, qb(k), k > 0 ? qb(k - 1) : nullptr,
-                                                      wbar, d_alpha, d_beta, AB, BB, K, k, bs, psw);
+                                                      wbar, d_alpha, d_beta, AB, BB, K, k, bs, pracc, psw);
         launch_bmv(p, B, d_theta, d_diag, wbar, tmp, bs.m, 2, k, s);
         ED_CHECK_LAUNCH_N("ed_batch_tape_reverse step", 3);
       }
@@ -762,8 +779,9 @@ ED_API ed_status ed_batch_tape_reverse(ed_plan p, int B, const double* d_theta, 
   k_bt_radot<<<gv, BT_NT, 0, s>>>(qb(0), tmp, d_ext_vec, d_ext_coef, q0, nullptr, nullptr, D, d_beta, AB, BB, K, -1,
                                   part, bs, res);
   k_bt_startbar<<<gv, BT_NT, 0, s>>>(qb(0), q0, D, d_beta, BB, K, res, bs, d_start_bar);
+  k_bt_diag_terms<<<gw, SW_NT, sandwich_smem(P), s>>>(g, p->n_sites, P, pracc, bs, psw);
   k_bt_param_reduce<<<B, SW_P, 0, s>>>(psw, L.nsw, P, d_theta_bar);
-  ED_CHECK_LAUNCH_N("ed_batch_tape_reverse final", 3);
+  ED_CHECK_LAUNCH_N("ed_batch_tape_reverse final", 4);
   return ED_OK;
 }
 
