@@ -1,0 +1,63 @@
+"""Small, self-contained workloads for profiling single kernels (ncu captures want one kernel
+on a few GB of device memory, not the whole benchmark step).
+
+    python -m cmpy_gb300.profile_cases gf14        # Green's-function Lanczos of the 14-site ring
+    python -m cmpy_gb300.profile_cases adjoint64   # batched adjoint, 64 SIAMs 1+9, forward + backward
+
+gf14: the particle-sector Lanczos of the 14-site Hubbard ring (U=4, mu=2, t=1), sector (8,7),
+D = 10,306,296, from a seeded uniform start vector, 12 steps in block fixed point (three
+rotating vectors, ~0.5 GB on the device): the update kernel and the integer matvec of the
+benchmark step, without its 23.6 GB Krylov store.
+adjoint64: the workload of the benchmark's `adjoint` extra (batched part): 64 SIAMs with
+1 impurity + 9 bath sites, sector (5,5), 1024 Matsubara frequencies at beta=100, seeded bath
+parameters (numpy default_rng(5)), forward and backward once.
+"""
+
+from __future__ import annotations
+
+import sys
+
+
+def gf14(steps: int = 12) -> None:
+    import torch
+
+    from . import engine as E
+    from .models import ChainLattice, HubbardModel
+
+    m = HubbardModel(ChainLattice(14, True), inter=4.0, mu=2.0, hop=1.0)
+    p = m.plan(8, 7)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    s = torch.rand(p.dim, dtype=torch.float64, device="cuda", generator=g)
+    a, b, _ = E.lanczos_coeffs(p, s, max_steps=steps)
+    torch.cuda.synchronize()
+    print(f"gf14: {a.numel()} steps, alpha_0 = {float(a[0]):.12f}")
+
+
+def adjoint64(n: int = 64) -> None:
+    import numpy as np
+    import torch
+
+    from .adjoint import greens_function_ad_batch, siam_parameters
+
+    rng = np.random.default_rng(5)
+    z = 1j * (2 * np.arange(1024) + 1) * np.pi / 100.0
+    eb = torch.tensor(rng.uniform(-2, 2, (n, 9)), dtype=torch.float64, device="cuda", requires_grad=True)
+    v = torch.tensor(rng.uniform(0.1, 0.6, (n, 9)), dtype=torch.float64, device="cuda", requires_grad=True)
+    u = torch.tensor(4.0, dtype=torch.float64, device="cuda")
+    e_imp = torch.tensor(0.0, dtype=torch.float64, device="cuda")
+    rows = [siam_parameters(u, e_imp, eb[i], v[i]) for i in range(n)]
+    th = torch.stack([r[0] for r in rows])
+    n_sites, bonds, width = rows[0][1], rows[0][2], rows[0][3]
+    g = greens_function_ad_batch(th, n_sites, bonds, (5, 5), z, sign_width=width, gs_steps=250, gf_levels=150,
+                                 ckpt=16)
+    torch.sum(torch.abs(g) ** 2).backward()
+    torch.cuda.synchronize()
+    print(f"adjoint64: |grad| = {float(eb.grad.abs().sum() + v.grad.abs().sum()):.6f}")
+
+
+CASES = {"gf14": gf14, "adjoint64": adjoint64}
+
+if __name__ == "__main__":
+    if len(sys.argv) != 2 or sys.argv[1] not in CASES:
+        sys.exit(f"usage: python -m cmpy_gb300.profile_cases {{{','.join(CASES)}}}")
+    CASES[sys.argv[1]]()
