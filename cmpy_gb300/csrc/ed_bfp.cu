@@ -946,8 +946,13 @@ __device__ __forceinline__ int64_t bfp_upd1(int64_t Aw, int64_t Aq, int64_t Ap, 
   add128(s, mul_s64(Aq, q));
   add128(s, mul_s64(Ap, pv));
   const int64_t r = shr128_round(s, SA);
-  add128(nrm, mul_s64(r, r));
-  mx = max(mx, uabs64(r));
+  // r^2 = |r|^2: the unsigned square (|r| < 2^63) needs no sign corrections of the high word
+  const unsigned long long ur = uabs64(r);
+  I128 sq;
+  sq.lo = ur * ur;
+  sq.hi = (int64_t)__umul64hi(ur, ur);
+  add128(nrm, sq);
+  mx = max(mx, ur);
   return r;
 }
 __device__ __forceinline__ longlong2 ld2_stream(const int64_t* p, uint64_t pol) {
