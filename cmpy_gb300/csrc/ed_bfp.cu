@@ -1043,21 +1043,7 @@ __global__ void __launch_bounds__(BT, 4) k_bfp_update(BfpVecs v, int k, const in
 }
 
 // ---- Ritz vector ------------------------------------------------------------------------------------
-// C_k = round(c_k / beta_k * 2^(e_k + SC)) with one SC for all k; psi = sum_k C_k R_k * 2^-SC
-__global__ void k_bfp_ritz_coeffs(const BfpVecs v, const double* c, const double* beta, const BfpState* st,
-                                  int64_t* C, int* SC_out) {
-  if (threadIdx.x != 0) return;
-  const int m = st->steps;
-  double gm = 0.0;
-  for (int k = 0; k < m; ++k) gm = fmax(gm, fabs(ldexp(c[k] / beta[k], v.eR[k])));
-  int eg = 0;
-  frexp(gm > 0.0 ? gm : 1.0, &eg);
-  // |C_k| < 2^62 - 10 bits of headroom for the sum over k
-  const int SC = 52 - eg;
-  for (int k = 0; k < m; ++k) C[k] = llrint(ldexp(c[k] / beta[k], v.eR[k] + SC));
-  *SC_out = SC;
-}
-
+// psi = sum_k C_k R_k * 2^-SC (C_k and SC from the host: see bfp_lanczos)
 __global__ void k_bfp_ritz(const BfpVecs v, const int64_t* __restrict__ C, const int* SCp, const BfpState* st,
                            double* __restrict__ out) {
   const int m = st->steps;
@@ -1474,32 +1460,6 @@ static BfpLayout bfp_layout(const ed_plan_s* p, int K, bool store) {
 
 size_t bfp_workspace_bytes(const ed_plan_s* p, int K, bool store) { return bfp_layout(p, K, store).total; }
 
-// T_m of the fixed-point run: alpha[0..m), couplings beta[1..m) (beta[0] is the start norm,
-// which tridiag_lowest_block never reads).
-__global__ void k_lz_check_bfp(const double* alpha, const double* beta, int k, double tol, BfpState* st, double* c,
-                               double* work) {
-  if (*(volatile int*)&st->stop) return;
-  const double e = tridiag_lowest_block<512>(alpha, beta, k + 1, c, work);
-  if (threadIdx.x == 0) {
-    const double res = fabs(beta[k + 1] * c[k]);
-    if (res <= tol * fmax(1.0, fabs(e))) { st->stop = 1; st->steps = k + 1; }
-    st->e_prev = e;
-    st->energy = e;
-    st->residual = res;
-  }
-}
-
-__global__ void k_lz_final_bfp(const double* alpha, const double* beta, int kmax, BfpState* st, double* c,
-                               double* work) {
-  const int m = st->stop ? st->steps : kmax;
-  const double e = tridiag_lowest_block<512>(alpha, beta, m, c, work);
-  if (threadIdx.x == 0) {
-    st->energy = e;
-    st->steps = m;
-    st->residual = fabs(beta[m] * c[m - 1]);
-  }
-}
-
 struct BfpRun {
   BfpLayout L;
   BfpVecs v;
@@ -1611,7 +1571,11 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
     ev.resize(2 * (size_t)Km);
     for (auto& e : ev) ED_CUDA(cudaEventCreate(&e));
   }
-  for (int k = 0; k < Km; ++k) {
+  // convergence tests and the final eigenpair of T run on the host (a chain of dependent FP64
+  // operations: tens of µs on a host core, milliseconds in one block of this GPU)
+  std::vector<double> ha, hb, hc;
+  int m_conv = 0, launched = 0;
+  for (int k = 0; k < Km && !m_conv; ++k) {
     if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k], s));
     const BfpFuse fz = bfp_fuse(p, r, k, alpha, beta);
     bool fused = false;
@@ -1621,33 +1585,60 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
       k_bfp_scalars<<<1, BT, 0, s>>>(r.v, k, p->bfp.F, p->bfp.m_in, r.part, r.partmax, bfp_matvec_grid(p), alpha,
                                      beta, r.st);
     ED_TRY(launch_update(p, r, k, alpha, beta, s));
-    uint64_t nl = fused ? 1 : 2;
-    if (prm->check_every > 0 && ((k + 1) % prm->check_every == 0) && k + 1 < Km) {
-      k_lz_check_bfp<<<1, 256, 0, s>>>(alpha, beta, k, prm->tol, r.st, r.c, r.work);
-      ++nl;
+    ED_CHECK_LAUNCH_N("bfp lanczos step", fused ? 1 : 2);
+    launched = k + 1;
+    if (prm->check_every > 0 && prm->tol > 0.0 && ((k + 1) % prm->check_every == 0) && k + 1 < Km) {
+      int hstop = 0;
+      ha.resize(k + 1);
+      hb.resize(k + 2);
+      ED_CUDA(cudaMemcpyAsync(&hstop, &r.st->stop, sizeof(int), cudaMemcpyDeviceToHost, s));
+      ED_CUDA(cudaMemcpyAsync(ha.data(), alpha, (k + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+      ED_CUDA(cudaMemcpyAsync(hb.data(), beta, (k + 2) * sizeof(double), cudaMemcpyDeviceToHost, s));
+      ED_CUDA(cudaStreamSynchronize(s));
+      if (hstop) break;  // invariant subspace or a failed wait: the device state says which
+      const double e = host_tridiag_lowest(ha.data(), hb.data(), k + 1, hc);
+      if (std::fabs(hb[k + 1] * hc[k]) <= prm->tol * std::max(1.0, std::fabs(e))) m_conv = k + 1;
     }
-    ED_CHECK_LAUNCH_N("bfp lanczos step", nl);
-  }
-  k_lz_final_bfp<<<1, 256, 0, s>>>(alpha, beta, Km, r.st, r.c, r.work);
-  ED_CHECK_LAUNCH("k_lz_final_bfp");
-  if (evec) {
-    k_bfp_ritz_coeffs<<<1, 32, 0, s>>>(r.v, r.c, beta, r.st, r.C, r.misc);
-    k_bfp_ritz<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(r.v, r.C, r.misc, r.st, evec);
-    ED_CHECK_LAUNCH_N("bfp ritz", 2);
   }
   BfpState hs;
   ED_CUDA(cudaMemcpyAsync(&hs, r.st, sizeof(BfpState), cudaMemcpyDeviceToHost, s));
   ED_CUDA(cudaStreamSynchronize(s));
-  res->energy = hs.energy;
-  res->residual = hs.residual;
-  res->steps = hs.steps;
-  res->converged = hs.stop;
-  res->status = hs.status;
   if (hs.status == DEV_TIMEOUT) return fail(ED_ERR_TIMEOUT, "fixed-point matvec: a bounded wait for a row copy ran out");
+  const int m = hs.stop ? hs.steps : (m_conv ? m_conv : launched);
+  ha.resize(m);
+  hb.resize(m + 1);
+  ED_CUDA(cudaMemcpyAsync(ha.data(), alpha, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(hb.data(), beta, (m + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+  std::vector<int32_t> he(m);
+  if (evec) ED_CUDA(cudaMemcpyAsync(he.data(), r.v.eR, m * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  const double e0 = host_tridiag_lowest(ha.data(), hb.data(), m, hc);
+  if (evec) {
+    // Ritz coefficients C_k = round(c_k / beta_k * 2^(e_k + SC)), one SC for all k with
+    // |C_k| < 2^62 - 10 bits of headroom for the sum over k
+    double gm = 0.0;
+    for (int k = 0; k < m; ++k) gm = std::max(gm, std::fabs(std::ldexp(hc[k] / hb[k], he[k])));
+    int eg = 0;
+    std::frexp(gm > 0.0 ? gm : 1.0, &eg);
+    const int SC = 52 - eg;
+    std::vector<int64_t> hC(m);
+    for (int k = 0; k < m; ++k) hC[k] = std::llrint(std::ldexp(hc[k] / hb[k], he[k] + SC));
+    ED_CUDA(cudaMemcpyAsync(r.C, hC.data(), m * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    ED_CUDA(cudaMemcpyAsync(r.misc, &SC, sizeof(int), cudaMemcpyHostToDevice, s));
+    ED_CUDA(cudaMemcpyAsync(&r.st->steps, &m, sizeof(int), cudaMemcpyHostToDevice, s));
+    k_bfp_ritz<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(r.v, r.C, r.misc, r.st, evec);
+    ED_CHECK_LAUNCH("k_bfp_ritz");
+    ED_CUDA(cudaStreamSynchronize(s));  // the host arrays above are sources of the copies
+  }
+  res->energy = e0;
+  res->residual = std::fabs(hb[m] * hc[m - 1]);
+  res->steps = m;
+  res->converged = hs.stop ? hs.stop : (m_conv ? 1 : 0);
+  res->status = hs.status;
   res->matvec_ms = 0.0;
   res->matvecs = 0;
   if (prm->profile) {
-    for (int k = 0; k < hs.steps; ++k) {
+    for (int k = 0; k < m; ++k) {
       float ms = 0.f;
       ED_CUDA(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));
       res->matvec_ms += ms;

@@ -1,7 +1,9 @@
 // Device Lanczos: the ground state that cmpy obtains from ARPACK eigsh(k=1, which="SA")
 // (cmpy/exactdiag.py:24-43) and the Lanczos coefficients of cmpy/exactdiag.py:324-375,
-// run entirely on the GPU. All scalars (alpha, beta, norms, flags) stay in device memory;
-// the host only enqueues kernels, so control crosses host->device once per solve.
+// run on the GPU. The recurrence's scalars (alpha, beta, norms, flags) stay in device memory
+// and the host enqueues the steps without waiting; it reads the scalars only at the
+// convergence tests and at the end, where it solves the small tridiagonal eigenproblem (a
+// chain of dependent FP64 operations, which a host core runs far faster than one GPU block).
 //
 // Reductions are deterministic: each block writes a partial, the last block to arrive
 // (atomic ticket, no waiting) sums the partials in block order.
@@ -207,32 +209,6 @@ __global__ void k_multiaxpy(const double* __restrict__ Q, int64_t ldq, int m, co
   }
 }
 
-// convergence check after step k (T has size k+1): Ritz residual |beta_{k+1} * s_k| of the
-// lowest Ritz pair, relative to max(1, |E|)
-__global__ void k_lz_check(const double* alpha, const double* beta, int k, double tol, LzState* st, double* c,
-                           double* work) {
-  if (lz_stopped(st)) return;
-  const double e = tridiag_lowest_block<512>(alpha, beta, k + 1, c, work);
-  if (threadIdx.x == 0) {
-    const double res = fabs(beta[k + 1] * c[k]);
-    if (res <= tol * fmax(1.0, fabs(e))) { st->stop = 1; st->steps = k + 1; }
-    st->e_prev = e;
-    st->energy = e;
-    st->residual = res;
-  }
-}
-
-// final eigenpair of T_m; m = st->steps if stopped else kmax
-__global__ void k_lz_final(const double* alpha, const double* beta, int kmax, LzState* st, double* c, double* work) {
-  const int m = st->stop ? st->steps : kmax;
-  const double e = tridiag_lowest_block<512>(alpha, beta, m, c, work);
-  if (threadIdx.x == 0) {
-    st->energy = e;
-    st->steps = m;
-    st->residual = fabs(beta[m] * c[m - 1]);
-  }
-}
-
 __global__ void k_tridiag(const double* alpha, const double* beta, int m, double* value, double* vec, double* work) {
   const double e = tridiag_lowest_block<512>(alpha, beta, m, vec, work);
   if (threadIdx.x == 0) *value = e;
@@ -372,18 +348,11 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
   double* part = (double*)(base + L.off_partial);
   double* h = (double*)(base + L.off_h);
   double* c = (double*)(base + L.off_c);
-  double* twork = (double*)(base + L.off_work);
   double* scal = (double*)(base + L.off_scalars);
   LzState* st = (LzState*)(base + L.off_state);
   ED_CUDA(cudaMemsetAsync(st, 0, sizeof(LzState), s));
   ED_CUDA(cudaMemsetAsync(d_alpha, 0, K * sizeof(double), s));
   ED_CUDA(cudaMemsetAsync(d_beta, 0, (K + 1) * sizeof(double), s));
-  {
-    // e_prev = +inf so the first check never converges
-    const double inf = INFINITY;
-    ED_CUDA(cudaMemcpyAsync(&st->e_prev, &inf, sizeof(double), cudaMemcpyHostToDevice, s));
-    ED_CUDA(cudaStreamSynchronize(s));
-  }
   const int gv = nparts;
   const int gs = grid_for(D, 256, p->ctx->num_sms * 8);
   // reorthogonalisation dots: element chunks of ~1024 (>= 32 elements per lane per vector)
@@ -416,7 +385,11 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
   // the Krylov dimension cannot exceed D; without reorthogonalisation rounding would
   // otherwise keep beta alive past it
   const int Km = (int)std::min<int64_t>(K, D);
-  for (int k = 0; k < Km; ++k) {
+  // convergence tests and the final eigenpair of T run on the host (a chain of dependent FP64
+  // operations: tens of µs on a host core, milliseconds in one block of this GPU)
+  std::vector<double> ha, hb, hc;
+  int m_conv = 0, launched = 0;
+  for (int k = 0; k < Km && !m_conv; ++k) {
     double* q = qv(k);
     double* qp = k > 0 ? qv(k - 1) : nullptr;
     if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k], s));
@@ -434,33 +407,50 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
       }
     }
     k_scale<<<gs, 256, 0, s>>>(w, qv(k + 1), D, d_beta + k + 1, stopf);
-    if (prm->check_every > 0 && ((k + 1) % prm->check_every == 0) && k + 1 < Km) {
-      k_lz_check<<<1, LZ_NT, 0, s>>>(d_alpha, d_beta, k, prm->tol, st, c, twork);
-      ++nl;
-    }
     ED_CHECK_LAUNCH_N("lanczos step", nl);
-  }
-  k_lz_final<<<1, LZ_NT, 0, s>>>(d_alpha, d_beta, Km, st, c, twork);
-  ED_CHECK_LAUNCH("k_lz_final");
-  if (prm->want_vector) {
-    k_ritz<<<gs, 256, 0, s>>>(Q, D, c, st, d_evec, D);
-    k_dot<<<gv, LZ_NT, 0, s>>>(d_evec, d_evec, D, part, st, 0, scal, scal + 1, nullptr);
-    k_scale<<<gs, 256, 0, s>>>(d_evec, d_evec, D, scal + 1, nullptr);
-    ED_CHECK_LAUNCH_N("lanczos ritz", 3);
+    launched = k + 1;
+    if (prm->check_every > 0 && prm->tol > 0.0 && ((k + 1) % prm->check_every == 0) && k + 1 < Km) {
+      int hstop = 0;
+      ha.resize(k + 1);
+      hb.resize(k + 2);
+      ED_CUDA(cudaMemcpyAsync(&hstop, stopf, sizeof(int), cudaMemcpyDeviceToHost, s));
+      ED_CUDA(cudaMemcpyAsync(ha.data(), d_alpha, (k + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+      ED_CUDA(cudaMemcpyAsync(hb.data(), d_beta, (k + 2) * sizeof(double), cudaMemcpyDeviceToHost, s));
+      ED_CUDA(cudaStreamSynchronize(s));
+      if (hstop) break;  // invariant subspace
+      const double e = host_tridiag_lowest(ha.data(), hb.data(), k + 1, hc);
+      if (std::fabs(hb[k + 1] * hc[k]) <= prm->tol * std::max(1.0, std::fabs(e))) m_conv = k + 1;
+    }
   }
   LzState hs;
   ED_CUDA(cudaMemcpyAsync(&hs, st, sizeof(LzState), cudaMemcpyDeviceToHost, s));
   ED_CUDA(cudaStreamSynchronize(s));
-  res->energy = hs.energy;
-  res->residual = hs.residual;
-  res->steps = hs.steps;
-  res->converged = hs.stop;
+  const int m = hs.stop ? hs.steps : (m_conv ? m_conv : launched);
+  ha.resize(m);
+  hb.resize(m + 1);
+  ED_CUDA(cudaMemcpyAsync(ha.data(), d_alpha, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(hb.data(), d_beta, (m + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  const double e0 = host_tridiag_lowest(ha.data(), hb.data(), m, hc);
+  if (prm->want_vector) {
+    ED_CUDA(cudaMemcpyAsync(c, hc.data(), m * sizeof(double), cudaMemcpyHostToDevice, s));
+    ED_CUDA(cudaMemcpyAsync(&st->steps, &m, sizeof(int), cudaMemcpyHostToDevice, s));
+    k_ritz<<<gs, 256, 0, s>>>(Q, D, c, st, d_evec, D);
+    k_dot<<<gv, LZ_NT, 0, s>>>(d_evec, d_evec, D, part, st, 0, scal, scal + 1, nullptr);
+    k_scale<<<gs, 256, 0, s>>>(d_evec, d_evec, D, scal + 1, nullptr);
+    ED_CHECK_LAUNCH_N("lanczos ritz", 3);
+    ED_CUDA(cudaStreamSynchronize(s));  // the host arrays above are sources of the copies
+  }
+  res->energy = e0;
+  res->residual = std::fabs(hb[m] * hc[m - 1]);
+  res->steps = m;
+  res->converged = hs.stop ? hs.stop : (m_conv ? 1 : 0);
   res->status = hs.status;
   res->matvec_ms = 0.0;
   res->matvecs = 0;
   if (prm->profile) {
     // matvecs after a stop return immediately; count only the steps that ran
-    for (int k = 0; k < hs.steps; ++k) {
+    for (int k = 0; k < m; ++k) {
       float ms = 0.f;
       ED_CUDA(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));
       res->matvec_ms += ms;

@@ -3,46 +3,56 @@
 // cmpy/exactdiag.py:368-375. Shared by the FP64 and the fixed-point Lanczos drivers.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "ed_common.cuh"
 
 namespace ed {
 
 // ---- symmetric tridiagonal eigen-solver (one block) ----------------------------------------
-// Number of eigenvalues of T (alpha[0..m), beta[1..m)) below x: sign changes of the LDL^T
-// pivots, computed without divisions by rescaling a three-term recurrence.
-static __device__ int sturm_count(const double* a, const double* b, int m, double x) {
-  // p_i = (a_i - x) p_{i-1} - b_i^2 p_{i-2}; count sign changes of p_i / p_{i-1}
-  // a zero p_i is replaced by a tiny value of the opposite sign of p_{i-1} (a tiny negative
-  // pivot), the usual convention for an eigenvalue exactly at x
+// Number of eigenvalues of T (alpha[0..m), beta[1..m)) below x: sign changes of the sequence
+// p_i = (a_i - x) p_{i-1} - b_i^2 p_{i-2} (the leading principal minors of T - x, so
+// p_i / p_{i-1} are the LDL^T pivots), without divisions. A zero p_i is replaced by a tiny
+// value of the opposite sign of p_{i-1} (a tiny negative pivot, the usual convention for an
+// eigenvalue exactly at x); the pair is rescaled by an exact power of two when p_i leaves
+// [2^-400, 2^400]. The signs, the zero test and the exponent are read from the bit patterns
+// (integer operations), so the FP64 pipe, narrow on this GPU, only runs the recurrence.
+// bb = b^2 when precomputed (may be null).
+static __device__ int sturm_count(const double* a, const double* b, const double* bb, int m, double x) {
   double p0 = 1.0, p1 = a[0] - x;
-  if (p1 == 0.0) p1 = -0x1.0p-900;
-  int cnt = (p1 < 0.0) ? 1 : 0;
+  long long s1 = __double_as_longlong(p1);
+  if ((s1 << 1) == 0) { p1 = -0x1.0p-900; s1 = __double_as_longlong(p1); }
+  int cnt = (int)((unsigned long long)s1 >> 63);
   for (int i = 1; i < m; ++i) {
-    const double bb = b[i] * b[i];
-    double p2 = (a[i] - x) * p1 - bb * p0;
-    if (p2 == 0.0) p2 = -p1 * 0x1.0p-60;
-    if ((p2 < 0.0) != (p1 < 0.0)) ++cnt;
-    // rescale to avoid overflow/underflow (exact powers of two)
-    const double ap = fabs(p2);
-    if (ap > 0x1.0p+400 || ap < 0x1.0p-400) {
-      const int e = ilogb(ap);
-      p2 = scalbn(p2, -e);
-      p1 = scalbn(p1, -e);
+    const double bbi = bb ? bb[i] : b[i] * b[i];
+    double p2 = fma(a[i] - x, p1, -bbi * p0);
+    long long s2 = __double_as_longlong(p2);
+    if ((s2 << 1) == 0) { p2 = -p1 * 0x1.0p-60; s2 = __double_as_longlong(p2); }
+    cnt += (int)((unsigned long long)(s2 ^ s1) >> 63);
+    const int ex = (int)((s2 >> 52) & 0x7ff);
+    if (ex > 1023 + 400 || ex < 1023 - 400) {
+      const double sc = __longlong_as_double((long long)(2046 - ex) << 52);  // 2^-(ex - 1023)
+      p2 *= sc;
+      p1 *= sc;
     }
     p0 = p1;
     p1 = p2;
+    s1 = s2;
   }
   return cnt;
 }
 
-// Lowest eigenvalue by 32-way multisection (warp 0 evaluates the Sturm counts; FP64 is a
-// scarce pipe on this GPU, so fewer points per round cost less in total), then optionally
-// the eigenvector by inverse iteration (thread 0, FP64, partial pivoting).
-constexpr int MS_PTS = 32;
+// Lowest eigenvalue by 128-way multisection (four warps evaluate the Sturm counts, one per
+// SM sub-partition: a warp's FP64 recurrence is bound by its sub-partition's FP64 pipe, so
+// more points per warp would not come for free), then optionally the eigenvector by inverse
+// iteration (thread 0, FP64, partial pivoting). Needs blockDim.x >= MS_PTS.
+constexpr int MS_PTS = 128;
 //
-// SM_M > 0 (single-block callers): for m <= SM_M the tridiagonal, the elimination work and the
-// vector live in static shared memory (7 * SM_M doubles) instead of global memory, which takes
-// the inverse iteration's dependent loads off the L2 round trip. Batched callers keep SM_M = 0.
+// SM_M > 0 (single-block callers): for m <= SM_M the tridiagonal (with b^2), the elimination
+// work and the vector live in static shared memory instead of global memory. Batched callers
+// keep SM_M = 0.
 template <int SM_M = 0>
 static __device__ double tridiag_lowest_block(const double* a_g, const double* b_g, int m, double* vec_g,
                                               double* work_g) {
@@ -50,21 +60,24 @@ static __device__ double tridiag_lowest_block(const double* a_g, const double* b
   __shared__ int cnt_s[MS_PTS];
   const double* a = a_g;
   const double* b = b_g;
+  const double* bb = nullptr;
   double* vec = vec_g;
   double* work = work_g;
   bool in_smem = false;
   if constexpr (SM_M > 0) {
-    __shared__ double s_ab[2 * SM_M];
+    __shared__ double s_ab[3 * SM_M];
     __shared__ double s_w[5 * SM_M];
     __shared__ double s_v[SM_M];
     if (m <= SM_M) {
       for (int i = threadIdx.x; i < m; i += blockDim.x) {
         s_ab[i] = a_g[i];
         s_ab[SM_M + i] = b_g[i];
+        s_ab[2 * SM_M + i] = b_g[i] * b_g[i];
       }
       __syncthreads();
       a = s_ab;
       b = s_ab + SM_M;
+      bb = s_ab + 2 * SM_M;
       work = s_w;
       if (vec_g) vec = s_v;
       in_smem = true;
@@ -86,7 +99,7 @@ static __device__ double tridiag_lowest_block(const double* a_g, const double* b
     const double lo = lo_s, hi = hi_s;
     if (threadIdx.x < MS_PTS) {
       const double x = lo + (hi - lo) * (double)(threadIdx.x + 1) / (double)(MS_PTS + 1);
-      cnt_s[threadIdx.x] = sturm_count(a, b, m, x);
+      cnt_s[threadIdx.x] = sturm_count(a, b, bb, m, x);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -102,41 +115,48 @@ static __device__ double tridiag_lowest_block(const double* a_g, const double* b
   }
   const double ev = 0.5 * (lo_s + hi_s);
   if (vec && threadIdx.x == 0) {
-    // inverse iteration: (T - ev I) y = v, Gaussian elimination with partial pivoting.
-    // work: 5*m doubles (diag, super, super2, sub multipliers, pivot flags)
-    double* dd = work;           // diagonal of U
+    // inverse iteration: (T - ev I) y = v, Gaussian elimination with partial pivoting, factored
+    // once; the pivots are kept as reciprocals, so the whole solve takes m FP64 divisions (the
+    // FP64 pipe of this GPU is narrow and a division is a long dependent sequence on it).
+    // work: 5*m doubles (reciprocal pivots, super, super2, sub multipliers, pivot flags)
+    double* dd = work;           // diagonal of U, then its reciprocals
     double* du = work + m;       // first super-diagonal of U
     double* du2 = work + 2 * m;  // second super-diagonal of U
     double* ml = work + 3 * m;   // multipliers
     double* pv = work + 4 * m;   // 1.0 if rows swapped at step i
     const double tiny = 1e-300 + 1e-15 * fmax(fabs(ev), 1.0) * 1e-3;
     for (int i = 0; i < m; ++i) vec[i] = 1.0 / sqrt((double)m) * (1.0 + 0.01 * (double)((i * 7919) % 13) / 13.0);
-    for (int it = 0; it < 3; ++it) {
-      // factor T - ev I (rebuilt each iteration; m is small)
-      for (int i = 0; i < m; ++i) { dd[i] = a[i] - ev; du[i] = (i + 1 < m) ? b[i + 1] : 0.0; du2[i] = 0.0; }
-      for (int i = 0; i < m - 1; ++i) {
-        const double sub = b[i + 1];
-        if (fabs(dd[i]) >= fabs(sub)) {
-          pv[i] = 0.0;
-          if (dd[i] == 0.0) dd[i] = tiny;
-          const double l = sub / dd[i];
-          ml[i] = l;
-          dd[i + 1] -= l * du[i];
-        } else {
-          pv[i] = 1.0;
-          const double l = dd[i] / sub;
-          ml[i] = l;
-          // swap rows i and i+1
-          const double t0 = dd[i + 1], t1 = (i + 2 < m) ? du[i + 1] : 0.0;
-          dd[i] = sub;
-          const double odu = du[i];
-          du[i] = t0;
-          du2[i] = t1;
-          dd[i + 1] = odu - l * t0;
-          if (i + 2 < m) du[i + 1] = -l * t1;
-        }
+    for (int i = 0; i < m; ++i) { dd[i] = a[i] - ev; du[i] = (i + 1 < m) ? b[i + 1] : 0.0; du2[i] = 0.0; }
+    // magnitude comparisons and zero tests on the bit patterns (integer operations)
+    const long long mag = 0x7fffffffffffffffll;
+    for (int i = 0; i < m - 1; ++i) {
+      const double sub = b[i + 1];
+      if ((__double_as_longlong(dd[i]) & mag) >= (__double_as_longlong(sub) & mag)) {
+        pv[i] = 0.0;
+        if ((__double_as_longlong(dd[i]) & mag) == 0) dd[i] = tiny;
+        const double r = 1.0 / dd[i];
+        const double l = sub * r;
+        ml[i] = l;
+        dd[i + 1] -= l * du[i];
+        dd[i] = r;
+      } else {
+        pv[i] = 1.0;
+        const double r = 1.0 / sub;
+        const double l = dd[i] * r;
+        ml[i] = l;
+        // swap rows i and i+1
+        const double t0 = dd[i + 1], t1 = (i + 2 < m) ? du[i + 1] : 0.0;
+        const double odu = du[i];
+        du[i] = t0;
+        du2[i] = t1;
+        dd[i + 1] = odu - l * t0;
+        if (i + 2 < m) du[i + 1] = -l * t1;
+        dd[i] = r;
       }
-      if (dd[m - 1] == 0.0) dd[m - 1] = tiny;
+    }
+    if (dd[m - 1] == 0.0) dd[m - 1] = tiny;
+    dd[m - 1] = 1.0 / dd[m - 1];
+    for (int it = 0; it < 2; ++it) {
       // forward: apply L^-1 to vec
       for (int i = 0; i < m - 1; ++i) {
         if (pv[i] != 0.0) { const double t = vec[i]; vec[i] = vec[i + 1]; vec[i + 1] = t - ml[i] * vec[i]; }
@@ -147,7 +167,7 @@ static __device__ double tridiag_lowest_block(const double* a_g, const double* b
         double s = vec[i];
         if (i + 1 < m) s -= du[i] * vec[i + 1];
         if (i + 2 < m) s -= du2[i] * vec[i + 2];
-        vec[i] = s / dd[i];
+        vec[i] = s * dd[i];
       }
       double nrm = 0.0;
       for (int i = 0; i < m; ++i) nrm = fma(vec[i], vec[i], nrm);
@@ -164,6 +184,86 @@ static __device__ double tridiag_lowest_block(const double* a_g, const double* b
     for (int i = threadIdx.x; i < m; i += blockDim.x) vec_g[i] = vec[i];
     __syncthreads();
   }
+  return ev;
+}
+
+// ---- the same on the host ----------------------------------------------------------------------
+// Lowest eigenpair of the tridiagonal (a[0..m), b[1..m)) on the host, FP64: bisection on the
+// Sturm count of the LDL^T pivots, then two steps of inverse iteration (Gaussian elimination
+// with partial pivoting); eigenvector sign: first nonzero component positive. The Lanczos
+// drivers use it for their convergence tests and final eigenpairs: the solve is a chain of
+// dependent FP64 operations, which this GPU's narrow FP64 pipe runs far slower (m = 250:
+// ~1.7 ms in one block) than a host core (tens of µs).
+inline double host_tridiag_lowest(const double* a, const double* b, int m, std::vector<double>& c) {
+  double lo = a[0], hi = a[0];
+  for (int i = 0; i < m; ++i) {
+    const double r = (i > 0 ? std::fabs(b[i]) : 0.0) + (i + 1 < m ? std::fabs(b[i + 1]) : 0.0);
+    lo = std::min(lo, a[i] - r);
+    hi = std::max(hi, a[i] + r);
+  }
+  const double pad = 1e-12 * std::max(std::fabs(lo), std::fabs(hi)) + 1e-300;
+  lo -= pad;
+  hi += pad;
+  auto count = [&](double x) {
+    int n = 0;
+    double q = a[0] - x;
+    for (int i = 0;;) {
+      if (q == 0.0) q = -1e-300;
+      if (q < 0.0) ++n;
+      if (++i >= m) break;
+      q = (a[i] - x) - b[i] * b[i] / q;
+    }
+    return n;
+  };
+  for (int it = 0; it < 200 && hi - lo > 4e-16 * std::max(std::fabs(lo), std::fabs(hi)) + 1e-300; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (count(mid) >= 1) hi = mid; else lo = mid;
+  }
+  const double ev = 0.5 * (lo + hi);
+  c.assign(m, 1.0 / std::sqrt((double)m));
+  for (int i = 0; i < m; ++i) c[i] *= 1.0 + 0.01 * (double)((i * 7919) % 13) / 13.0;
+  std::vector<double> dd(m), du(m), du2(m), ml(m);
+  std::vector<char> pv(m);
+  const double tiny = 1e-300 + 1e-18 * std::max(std::fabs(ev), 1.0);
+  for (int it = 0; it < 2; ++it) {
+    for (int i = 0; i < m; ++i) { dd[i] = a[i] - ev; du[i] = (i + 1 < m) ? b[i + 1] : 0.0; du2[i] = 0.0; }
+    for (int i = 0; i + 1 < m; ++i) {
+      const double sub = b[i + 1];
+      if (std::fabs(dd[i]) >= std::fabs(sub)) {
+        pv[i] = 0;
+        if (dd[i] == 0.0) dd[i] = tiny;
+        ml[i] = sub / dd[i];
+        dd[i + 1] -= ml[i] * du[i];
+      } else {
+        pv[i] = 1;
+        const double l = dd[i] / sub, t0 = dd[i + 1], t1 = (i + 2 < m) ? du[i + 1] : 0.0, odu = du[i];
+        ml[i] = l;
+        dd[i] = sub;
+        du[i] = t0;
+        du2[i] = t1;
+        dd[i + 1] = odu - l * t0;
+        if (i + 2 < m) du[i + 1] = -l * t1;
+      }
+    }
+    if (dd[m - 1] == 0.0) dd[m - 1] = tiny;
+    for (int i = 0; i + 1 < m; ++i) {
+      if (pv[i]) { const double t = c[i]; c[i] = c[i + 1]; c[i + 1] = t - ml[i] * c[i]; }
+      else c[i + 1] -= ml[i] * c[i];
+    }
+    for (int i = m - 1; i >= 0; --i) {
+      double s = c[i];
+      if (i + 1 < m) s -= du[i] * c[i + 1];
+      if (i + 2 < m) s -= du2[i] * c[i + 2];
+      c[i] = s / dd[i];
+    }
+    double nrm = 0.0;
+    for (int i = 0; i < m; ++i) nrm += c[i] * c[i];
+    nrm = 1.0 / std::sqrt(nrm);
+    for (int i = 0; i < m; ++i) c[i] *= nrm;
+  }
+  double sg = 1.0;
+  for (int i = 0; i < m; ++i) if (c[i] != 0.0) { sg = c[i] > 0 ? 1.0 : -1.0; break; }
+  for (int i = 0; i < m; ++i) c[i] *= sg;
   return ev;
 }
 
