@@ -358,7 +358,7 @@ def run_batched_sweep():
     fillings = list(m.basis.iter_fillings())
     plans = [m.plan(a, b) for a, b in fillings]
     b = Batch(plans)
-    th, ps, _ = b.tune(40)
+    th, ps, cs, _ = b.tune(40)
     b.lanczos(max_steps=300, tol=1e-12, check_every=10)  # warm
     res, t_batch = _timed(lambda: b.lanczos(max_steps=300, tol=1e-12, check_every=10))
     e_batch = res.energy.cpu().numpy()
@@ -379,7 +379,7 @@ def run_batched_sweep():
         "gs_energy": float(e_batch[i]),
         "gs_sector": list(fillings[i]),
         "max_rel_diff_vs_plain": float(np.max(np.abs(e_batch - e_plain) / np.maximum(1.0, np.abs(e_plain)))),
-        "tuned": {"threads": th, "ctas_per_sm": ps},
+        "tuned": {"threads": th, "ctas_per_sm": ps, "cluster_size": cs},
         "launches": "1 persistent batched kernel vs per-sector Lanczos sequences",
     }
 

@@ -143,14 +143,15 @@ _SIGNATURES = {
     "ed_tridiag_lowest_noalloc": (I32, [P, P, I32, P, P, P]),
     "ed_batch_create": (I32, [C.POINTER(C.c_void_p), I32, C.POINTER(C.c_void_p)]),
     "ed_batch_destroy": (I32, [C.c_void_p]),
-    "ed_batch_workspace": (I32, [C.c_void_p, I32, I32, I32, C.POINTER(C.c_size_t)]),
+    "ed_batch_workspace": (I32, [C.c_void_p, I32, I32, I32, I32, C.POINTER(C.c_size_t)]),
     "ed_batch_lanczos": (
         I32,
-        [C.c_void_p, I32, F64, I32, C.c_uint64, P, I32, P, C.c_size_t, P, P, P, P, P, P, P, I32, I32, P],
+        [C.c_void_p, I32, F64, I32, C.c_uint64, P, I32, P, C.c_size_t, P, P, P, P, P, P, P, I32, I32, I32, P],
     ),
     "ed_batch_tune": (
         I32,
-        [C.c_void_p, I32, P, C.c_size_t, P, P, P, P, P, C.POINTER(I32), C.POINTER(I32), C.POINTER(C.c_float), P],
+        [C.c_void_p, I32, P, C.c_size_t, P, P, P, P, P, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32),
+         C.POINTER(C.c_float), P],
     ),
     "ed_batch_gf_continued_fraction": (I32, [I32, I32, P, P, P, P, I32, P, I64, P, P]),
     "ed_plan_num_params": (I32, [PLAN]),

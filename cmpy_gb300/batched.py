@@ -49,6 +49,7 @@ class Batch:
         self._ws = torch.empty(0, dtype=torch.uint8, device=E.device())
         self.threads = 0
         self.ctas_per_sm = 0
+        self.cluster_size = 0
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -59,9 +60,10 @@ class Batch:
                 pass
             self._h = None
 
-    def workspace(self, max_steps: int, threads: int = 0, ctas_per_sm: int = 0) -> torch.Tensor:
+    def workspace(self, max_steps: int, threads: int = 0, ctas_per_sm: int = 0, cluster_size: int = 0) -> torch.Tensor:
         nb = C.c_size_t()
-        N.check(N.lib().ed_batch_workspace(self._h, int(max_steps), int(threads), int(ctas_per_sm), C.byref(nb)))
+        N.check(N.lib().ed_batch_workspace(self._h, int(max_steps), int(threads), int(ctas_per_sm), int(cluster_size),
+                                           C.byref(nb)))
         if self._ws.numel() < nb.value:
             self._ws = torch.empty(int(nb.value), dtype=torch.uint8, device=E.device())
         return self._ws
@@ -75,22 +77,24 @@ class Batch:
                 torch.empty(self.n, dtype=torch.int32, device=dev))
 
     def tune(self, tune_steps: int = 40):
-        """Pick threads-per-CTA and CTAs-per-SM by timing the candidates."""
+        """Pick threads per CTA, CTAs per SM and the cluster size per problem by timing the
+        candidates; returns (threads, ctas_per_sm, cluster_size, ms)."""
         # size the workspace for the largest candidate grid
         best = 0
-        for t, ps in ((128, 4), (256, 2), (256, 4), (512, 1), (512, 2), (1024, 1)):
+        for t, ps, cs in ((128, 4, 1), (256, 2, 1), (256, 4, 1), (512, 1, 1), (512, 2, 1), (1024, 1, 1),
+                          (512, 2, 2), (1024, 1, 2), (512, 2, 4), (1024, 1, 4), (512, 2, 8), (1024, 1, 8)):
             nb = C.c_size_t()
-            N.check(N.lib().ed_batch_workspace(self._h, int(tune_steps), t, ps, C.byref(nb)))
+            N.check(N.lib().ed_batch_workspace(self._h, int(tune_steps), t, ps, cs, C.byref(nb)))
             best = max(best, nb.value)
         if self._ws.numel() < best:
             self._ws = torch.empty(int(best), dtype=torch.uint8, device=E.device())
         a, b, e, r, s = self._outputs(tune_steps)
-        th, ps, ms = C.c_int(), C.c_int(), C.c_float()
+        th, ps, cs, ms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
         N.check(N.lib().ed_batch_tune(self._h, int(tune_steps), N.ptr(self._ws), self._ws.numel(), N.ptr(a), N.ptr(b),
-                                      N.ptr(e), N.ptr(r), N.ptr(s), C.byref(th), C.byref(ps), C.byref(ms),
-                                      E._stream()))
-        self.threads, self.ctas_per_sm = int(th.value), int(ps.value)
-        return self.threads, self.ctas_per_sm, float(ms.value)
+                                      N.ptr(e), N.ptr(r), N.ptr(s), C.byref(th), C.byref(ps), C.byref(cs),
+                                      C.byref(ms), E._stream()))
+        self.threads, self.ctas_per_sm, self.cluster_size = int(th.value), int(ps.value), int(cs.value)
+        return self.threads, self.ctas_per_sm, self.cluster_size, float(ms.value)
 
     def lanczos(self, max_steps: int = 300, tol: float = 1e-12, check_every: int = 10, seed: int = 0,
                 starts: Sequence[torch.Tensor] | None = None, want_vector: bool = False,
@@ -98,7 +102,7 @@ class Batch:
         """Ground states (and optionally vectors) of every problem. Asynchronous: the result
         tensors are filled on the current stream."""
         K = int(max_steps)
-        ws = self.workspace(K, self.threads, self.ctas_per_sm)
+        ws = self.workspace(K, self.threads, self.ctas_per_sm, self.cluster_size)
         if out is None:
             a, b, e, r, s = self._outputs(K)
             vecs = None
@@ -121,7 +125,7 @@ class Batch:
             self._h, K, float(tol), int(check_every), int(seed), starts_ptr, int(bool(want_vector)), N.ptr(ws),
             ws.numel(), N.ptr(out.alpha), N.ptr(out.beta), N.ptr(out.energy), N.ptr(out.residual), N.ptr(out.steps),
             N.ptr(self._vbuf) if want_vector else None, N.ptr(self._voff) if want_vector else None,
-            int(self.threads), int(self.ctas_per_sm), E._stream()))
+            int(self.threads), int(self.ctas_per_sm), int(self.cluster_size), E._stream()))
         return out
 
 

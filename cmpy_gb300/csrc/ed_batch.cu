@@ -12,13 +12,24 @@
 //
 // Vector arithmetic is the block-fixed-point scheme of ed_bfp.cu (int64 mantissas, one
 // exponent per vector, exact integer matvec, 128-bit dot products).
+//
+// With a thread-block cluster of CS > 1 CTAs per problem, the cluster's CTAs split the
+// elements of every vector loop (CTA rank r takes the r-th stripe of CS * NT) and exchange their
+// block totals through distributed shared memory at the hardware cluster barrier; every CTA
+// then holds the same totals and computes the same scalars, so all CTAs of a cluster take the
+// same branches and reach the same barriers. The largest sectors, which bound the makespan of
+// the work queue, thus run on CS SMs.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "ed_plan.cuh"
 #include "ed_tridiag.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace ed {
 
@@ -129,23 +140,73 @@ __device__ __forceinline__ unsigned long long bmax(unsigned long long v, BlockSc
   return r;
 }
 
+// Cluster-wide (sum, max) of values held per thread: block totals first, then (CS > 1) the CS
+// block totals through distributed shared memory, in rank order, so every CTA gets the same
+// result. xd / xu: two exchange slots each (alternating with `ph`: a slot is rewritten only
+// after a later cluster barrier, when every CTA has read it). The barrier also orders the
+// global-memory writes of the phase before it for all CTAs of the cluster.
+struct ClusterXch {
+  double* xd;
+  unsigned long long* xu;
+  int ph;
+};
+
+template <int NT, int CS>
+__device__ __forceinline__ void cred(double& sumv, unsigned long long& maxv, BlockScratch<NT>& s, ClusterXch& x) {
+  sumv = bsum<NT>(sumv, s);
+  maxv = bmax<NT>(maxv, s);
+  if constexpr (CS > 1) {
+    cg::cluster_group cl = cg::this_cluster();
+    if (threadIdx.x == 0) {
+      x.xd[x.ph] = sumv;
+      x.xu[x.ph] = maxv;
+    }
+    __threadfence();
+    cl.sync();
+    double t = 0.0;
+    unsigned long long m = 0;
+#pragma unroll
+    for (int q = 0; q < CS; ++q) {
+      t += *cl.map_shared_rank(x.xd + x.ph, q);
+      m = max(m, *cl.map_shared_rank(x.xu + x.ph, q));
+    }
+    sumv = t;
+    maxv = m;
+    x.ph ^= 1;
+  }
+}
+
+// a cluster barrier with global-memory ordering (no-op for CS = 1 beyond the block barrier)
+template <int CS>
+__device__ __forceinline__ void csync() {
+  if constexpr (CS > 1) {
+    __threadfence();
+    cg::this_cluster().sync();
+  } else {
+    __syncthreads();
+  }
+}
+
 __device__ __forceinline__ double start_value(const double* start, int64_t i, uint64_t seed) {
   if (start) return start[i];
   return (double)(bsplitmix(seed * 0x100000001B3ull + (uint64_t)i) >> 11) * 0x1.0p-53 + 0x1.0p-54;
 }
 
 // R0 = round(v0 * 2^-e), max |R0| < 2^m_in; returns e, writes ||v0|| and max |R0|
-template <int NT>
+// (elements i = rk * NT + tid, step CS * NT: this CTA's stripe)
+template <int NT, int CS>
 __device__ int batch_start(const BatchProblem& P, const double* start, int64_t* R0, uint64_t seed,
-                           BlockScratch<NT>& s, double* norm, unsigned long long* maxm) {
+                           BlockScratch<NT>& s, ClusterXch& x, int rk, double* norm, unsigned long long* maxm) {
   unsigned long long mb = 0;
   bool finite = true;
-  for (int64_t i = threadIdx.x; i < P.D; i += NT) {
+  for (int64_t i = (int64_t)rk * NT + threadIdx.x; i < P.D; i += (int64_t)CS * NT) {
     const double v = start_value(start, i, seed);
     finite &= (bool)isfinite(v);
     mb = max(mb, (unsigned long long)__double_as_longlong(fabs(v)));
   }
-  mb = bmax<NT>(finite ? mb : 0x7FF0000000000000ull, s);
+  double dummy = 0.0;
+  mb = finite ? mb : 0x7FF0000000000000ull;
+  cred<NT, CS>(dummy, mb, s, x);
   const double mx = __longlong_as_double((long long)mb);
   if (!isfinite(mx) || mx == 0.0) {
     *norm = isfinite(mx) ? 0.0 : NAN;
@@ -157,27 +218,29 @@ __device__ int batch_start(const BatchProblem& P, const double* start, int64_t* 
   const int e = e2 - P.m_in;
   I128 acc{0, 0};
   unsigned long long mm = 0;
-  for (int64_t i = threadIdx.x; i < P.D; i += NT) {
+  for (int64_t i = (int64_t)rk * NT + threadIdx.x; i < P.D; i += (int64_t)CS * NT) {
     const int64_t r = llrint(ldexp(start_value(start, i, seed), -e));
     R0[i] = r;
     add128(acc, mul_s64(r, r));
     mm = max(mm, uabs64(r));
   }
   __syncthreads();
-  const double t = bsum<NT>(i128_to_double(acc), s);
-  *maxm = bmax<NT>(mm, s);
+  double t = i128_to_double(acc);
+  cred<NT, CS>(t, mm, s, x);
+  *maxm = mm;
   *norm = ldexp(sqrt(t), e);
   return e;
 }
 
-// W = H X in integers; returns <X, W> (exact per thread, FP64 across threads), max |W|
-template <int NT>
+// W = H X in integers on this CTA's stripe of rows; returns <X, W> (exact per thread, FP64
+// across threads and CTAs), max |W|. X is read at every element (the hops reach other stripes).
+template <int NT, int CS>
 __device__ double batch_matvec(const BatchProblem& P, const int64_t* __restrict__ X, int64_t* __restrict__ W,
-                               BlockScratch<NT>& s, unsigned long long* maxw) {
+                               BlockScratch<NT>& s, ClusterXch& xc, int rk, unsigned long long* maxw) {
   I128 dot{0, 0};
   unsigned long long mx = 0;
   const int64_t nd = P.nd;
-  for (int64_t i = threadIdx.x; i < P.D; i += NT) {
+  for (int64_t i = (int64_t)rk * NT + threadIdx.x; i < P.D; i += (int64_t)CS * NT) {
     const int64_t u = i / nd, d = i - u * nd;
     const int64_t* xrow = X + u * nd;
     int64_t h = 0;
@@ -211,8 +274,9 @@ __device__ double batch_matvec(const BatchProblem& P, const int64_t* __restrict_
     mx = max(mx, uabs64(w));
   }
   __syncthreads();
-  const double t = bsum<NT>(i128_to_double(dot), s);
-  *maxw = bmax<NT>(mx, s);
+  double t = i128_to_double(dot);
+  cred<NT, CS>(t, mx, s, xc);
+  *maxw = mx;
   return t;
 }
 
@@ -243,20 +307,23 @@ __device__ StepCoef batch_coef(double a, double bk, double bkm1, int k, int ew, 
 
 // The Lanczos recurrence of one problem. Pass 1 (Ck == null) records alpha, beta and the
 // exponent of every R_k and stops on convergence / invariant subspace; pass 2 replays
-// exactly `m` steps and accumulates acc += Ck[k] * R_k.
-template <int NT>
+// exactly `m` steps and accumulates acc += Ck[k] * R_k. alpha / beta are this CTA's copies.
+template <int NT, int CS>
 __device__ void batch_recurrence(const BatchProblem& P, const double* start, uint64_t seed, int K, double tol,
-                                 int check_every, int64_t* Ra, int64_t* Rb, int64_t* W, double* alpha,
+                                 int check_every, int rk, int64_t* Ra, int64_t* Rb, int64_t* W, double* alpha,
                                  double* beta, double* c, double* work, int32_t* exps, int* m_io,
                                  const int64_t* Ck, uint64_t* acc_lo, int64_t* acc_hi) {
   __shared__ BlockScratch<NT> s;
   __shared__ int sh_stop, sh_m, sh_e0, sh_e1;
   __shared__ unsigned long long sh_m0, sh_m1;
   __shared__ StepCoef sh_c;
+  __shared__ double xd[2];
+  __shared__ unsigned long long xu[2];
+  ClusterXch xc{xd, xu, 0};
   const bool pass2 = Ck != nullptr;
   double nrm = 0.0;
   unsigned long long mstart = 0;
-  const int e_start = batch_start<NT>(P, start, Ra, seed, s, &nrm, &mstart);
+  const int e_start = batch_start<NT, CS>(P, start, Ra, seed, s, xc, rk, &nrm, &mstart);
   if (threadIdx.x == 0) {
     sh_stop = 0;
     sh_m = 0;
@@ -270,13 +337,14 @@ __device__ void batch_recurrence(const BatchProblem& P, const double* start, uin
     }
   }
   if (pass2)
-    for (int64_t i = threadIdx.x; i < P.D; i += NT) {
+    for (int64_t i = (int64_t)rk * NT + threadIdx.x; i < P.D; i += (int64_t)CS * NT) {
       acc_lo[i] = 0;
       acc_hi[i] = 0;
     }
   __syncthreads();
   if (!(nrm > 0.0)) {  // zero or non-finite start vector: empty Krylov space
     if (threadIdx.x == 0 && !pass2) *m_io = 0;
+    csync<CS>();  // m is read by every thread (and nrm is the same in every CTA of the cluster)
     return;
   }
   const int Km = (int)min((int64_t)K, P.D);
@@ -286,7 +354,7 @@ __device__ void batch_recurrence(const BatchProblem& P, const double* start, uin
   for (int k = 0; k < mlim; ++k) {
     if (pass2) {
       const int64_t C = Ck[k];
-      for (int64_t i = threadIdx.x; i < P.D; i += NT) {
+      for (int64_t i = (int64_t)rk * NT + threadIdx.x; i < P.D; i += (int64_t)CS * NT) {
         I128 v{acc_lo[i], acc_hi[i]};
         add128(v, mul_s64(C, Rk[i]));
         acc_lo[i] = v.lo;
@@ -295,7 +363,7 @@ __device__ void batch_recurrence(const BatchProblem& P, const double* start, uin
       if (k + 1 == mlim) break;
     }
     unsigned long long mw = 0;
-    const double dot = batch_matvec<NT>(P, Rk, W, s, &mw);
+    const double dot = batch_matvec<NT, CS>(P, Rk, W, s, xc, rk, &mw);
     if (threadIdx.x == 0) {
       const int ek = sh_e1, ew = ek - P.F;
       const double bk = beta[k];
@@ -308,7 +376,7 @@ __device__ void batch_recurrence(const BatchProblem& P, const double* start, uin
     const StepCoef cf = sh_c;
     I128 nn{0, 0};
     unsigned long long mx = 0;
-    for (int64_t i = threadIdx.x; i < P.D; i += NT) {
+    for (int64_t i = (int64_t)rk * NT + threadIdx.x; i < P.D; i += (int64_t)CS * NT) {
       I128 t = mul_s64(cf.Aw, W[i]);
       add128(t, mul_s64(cf.Aq, Rk[i]));
       if (k > 0) add128(t, mul_s64(cf.Ap, Rp[i]));
@@ -318,8 +386,9 @@ __device__ void batch_recurrence(const BatchProblem& P, const double* start, uin
       mx = max(mx, uabs64(r));
     }
     __syncthreads();
-    const double t2 = bsum<NT>(i128_to_double(nn), s);
-    mx = bmax<NT>(mx, s);
+    // the cluster exchange also orders every CTA's R_{k+1} stripe before the next matvec
+    double t2 = i128_to_double(nn);
+    cred<NT, CS>(t2, mx, s, xc);
     if (threadIdx.x == 0) {
       const double bn = ldexp(sqrt(t2), cf.er);
       if (!pass2) {
@@ -343,6 +412,7 @@ __device__ void batch_recurrence(const BatchProblem& P, const double* start, uin
     if (!pass2) {
       if (sh_stop) break;
       if (check_every > 0 && (k + 1) % check_every == 0 && k + 1 < Km) {
+        // every CTA of the cluster solves the same tridiagonal (same data, same result)
         const double e = tridiag_lowest_block(alpha, beta, k + 1, c, work);
         if (threadIdx.x == 0) {
           const double res = fabs(beta[k + 1] * c[k]);
@@ -358,84 +428,101 @@ __device__ void batch_recurrence(const BatchProblem& P, const double* start, uin
   }
   __syncthreads();
   if (!pass2 && threadIdx.x == 0) *m_io = sh_stop ? sh_m : Km;
-  __syncthreads();
+  csync<CS>();  // the pass's last vector writes, ordered before what follows
 }
 
-template <int NT>
+template <int NT, int CS>
 __global__ void __launch_bounds__(NT) k_batch_lanczos(const BatchProblem* __restrict__ probs,
                                                       const int* __restrict__ order, int n, int K, double tol,
                                                       int check_every, uint64_t seed,
                                                       const double* const* __restrict__ starts, int want_vector,
                                                       BatchOut out, BatchWork wk) {
   __shared__ int sh_p, sh_m, sh_sc;
-  int64_t* Ra = wk.slots + (int64_t)blockIdx.x * 5 * wk.dmax;
+  __shared__ BlockScratch<NT> s2;
+  __shared__ double xd2[2];
+  __shared__ unsigned long long xu2[2];
+  const int rk = CS > 1 ? (int)(blockIdx.x % CS) : 0;
+  const int64_t cid = blockIdx.x / CS;  // the cluster's vector slots
+  int64_t* Ra = wk.slots + cid * 5 * wk.dmax;
   int64_t* Rb = Ra + wk.dmax;
   int64_t* W = Rb + wk.dmax;
   uint64_t* acc_lo = (uint64_t*)(W + wk.dmax);
   int64_t* acc_hi = (int64_t*)(acc_lo + wk.dmax);
-  double* work = wk.tri + (int64_t)blockIdx.x * 6 * (K + 2);
+  // this CTA's tridiagonal work, eigenvector and copies of alpha, beta
+  double* work = wk.tri + (int64_t)blockIdx.x * 8 * (K + 2);
   double* c = work + 5 * (K + 2);
+  double* al = c + (K + 2);
+  double* be = al + (K + 2);
   int32_t* exps = wk.exps + (int64_t)blockIdx.x * (K + 2);
   int64_t* Ck = wk.coefs + (int64_t)blockIdx.x * (K + 2);
   while (true) {
-    if (threadIdx.x == 0) sh_p = atomicAdd(wk.queue, 1);
-    __syncthreads();
-    const int q = sh_p;
-    __syncthreads();
+    // rank 0 pulls the next problem; every CTA of the cluster reads it from rank 0
+    if (threadIdx.x == 0 && rk == 0) sh_p = atomicAdd(wk.queue, 1);
+    csync<CS>();
+    int q;
+    if constexpr (CS > 1) q = *cg::this_cluster().map_shared_rank(&sh_p, 0);
+    else q = sh_p;
+    csync<CS>();
     if (q >= n) break;
     const int p = order[q];
     const BatchProblem& P = probs[p];
     const double* start = starts ? starts[p] : nullptr;
-    double* alpha = out.alpha + (int64_t)p * K;
-    double* beta = out.beta + (int64_t)p * (K + 1);
     const uint64_t sd = seed + 0x9E37ull * (uint64_t)p;
-    batch_recurrence<NT>(P, start, sd, K, tol, check_every, Ra, Rb, W, alpha, beta, c, work, exps, &sh_m, nullptr,
-                         nullptr, nullptr);
+    batch_recurrence<NT, CS>(P, start, sd, K, tol, check_every, rk, Ra, Rb, W, al, be, c, work, exps, &sh_m,
+                             nullptr, nullptr, nullptr);
     const int m = sh_m;
+    if (rk == 0) {
+      double* alpha = out.alpha + (int64_t)p * K;
+      double* beta = out.beta + (int64_t)p * (K + 1);
+      for (int k = threadIdx.x; k < m; k += NT) alpha[k] = al[k];
+      for (int k = threadIdx.x; k <= m; k += NT) beta[k] = be[k];
+    }
     if (m == 0) {
-      if (threadIdx.x == 0) {
+      if (threadIdx.x == 0 && rk == 0) {
         out.energy[p] = NAN;
         out.residual[p] = 0.0;
         out.steps[p] = 0;
       }
-      __syncthreads();
       continue;
     }
-    const double e = tridiag_lowest_block(alpha, beta, m, c, work);
-    if (threadIdx.x == 0) {
+    const double e = tridiag_lowest_block(al, be, m, c, work);
+    if (threadIdx.x == 0 && rk == 0) {
       out.energy[p] = e;
-      out.residual[p] = fabs(beta[m] * c[m - 1]);
+      out.residual[p] = fabs(be[m] * c[m - 1]);
       out.steps[p] = m;
     }
     if (want_vector && out.vec) {
       // psi = sum_k (c_k / beta_k) R_k,  R_k = Rm_k 2^e_k:  C_k = round(c_k/beta_k 2^(e_k + SC))
       if (threadIdx.x == 0) {
         double gm = 0.0;
-        for (int k = 0; k < m; ++k) gm = fmax(gm, fabs(ldexp(c[k] / beta[k], exps[k])));
+        for (int k = 0; k < m; ++k) gm = fmax(gm, fabs(ldexp(c[k] / be[k], exps[k])));
         int eg = 0;
         frexp(gm > 0.0 ? gm : 1.0, &eg);
         sh_sc = 52 - eg;
-        for (int k = 0; k < m; ++k) Ck[k] = llrint(ldexp(c[k] / beta[k], exps[k] + sh_sc));
+        for (int k = 0; k < m; ++k) Ck[k] = llrint(ldexp(c[k] / be[k], exps[k] + sh_sc));
       }
       __syncthreads();
       int mm = m;
-      batch_recurrence<NT>(P, start, sd, K, tol, check_every, Ra, Rb, W, alpha, beta, c, work, exps, &mm, Ck, acc_lo,
-                           acc_hi);
+      batch_recurrence<NT, CS>(P, start, sd, K, tol, check_every, rk, Ra, Rb, W, al, be, c, work, exps, &mm, Ck,
+                               acc_lo, acc_hi);
       // normalise and write FP64
-      __shared__ BlockScratch<NT> s2;
       double sq = 0.0;
       const int sc = sh_sc;
-      for (int64_t i = threadIdx.x; i < P.D; i += NT) {
+      for (int64_t i = (int64_t)rk * NT + threadIdx.x; i < P.D; i += (int64_t)CS * NT) {
         const double v = ldexp(i128_to_double(I128{acc_lo[i], acc_hi[i]}), -sc);
         sq = fma(v, v, sq);
       }
-      const double inv = 1.0 / sqrt(bsum<NT>(sq, s2));
+      ClusterXch xc{xd2, xu2, 0};
+      unsigned long long dummy = 0;
+      cred<NT, CS>(sq, dummy, s2, xc);
+      const double inv = 1.0 / sqrt(sq);
       double* vo = out.vec + out.vec_off[p];
-      for (int64_t i = threadIdx.x; i < P.D; i += NT)
+      for (int64_t i = (int64_t)rk * NT + threadIdx.x; i < P.D; i += (int64_t)CS * NT)
         vo[i] = ldexp(i128_to_double(I128{acc_lo[i], acc_hi[i]}), -sc) * inv;
     }
-    __syncthreads();
+    csync<CS>();  // the cluster's slots are free for the next problem
   }
+  csync<CS>();  // no CTA leaves while another may still read its shared memory
 }
 
 // G_p(z) += sign * norm_p^2 / (z' - a0 - b1^2 / (z' - a1 - ...)),  z' = sign*z + e0_p,
@@ -483,12 +570,15 @@ struct ed_batch_s {
   ed::DeviceContext* ctx = nullptr;
   int tuned_threads = 0;
   int tuned_per_sm = 0;
+  int tuned_cluster = 0;
 };
 
 namespace ed {
 
-static int batch_grid(const ed_batch_s* b, int per_sm) {
-  return std::max(1, std::min(b->n, b->ctx->num_sms * per_sm));
+// the grid: clusters of cs CTAs, at most one cluster per problem and per_sm CTAs per SM
+static int batch_grid(const ed_batch_s* b, int per_sm, int cs) {
+  const int clusters = std::max(1, std::min(b->n, b->ctx->num_sms * per_sm / cs));
+  return clusters * cs;
 }
 
 struct BatchLayout {
@@ -497,33 +587,57 @@ struct BatchLayout {
 
 static size_t al256b(size_t x) { return (x + 255) & ~(size_t)255; }
 
-static BatchLayout batch_layout(const ed_batch_s* b, int K, int grid) {
+// vector slots per cluster; tridiagonal work, eigenvector, alpha/beta copies, exponents and
+// Ritz coefficients per CTA
+static BatchLayout batch_layout(const ed_batch_s* b, int K, int grid, int cs) {
   BatchLayout L;
   size_t o = 0;
   L.off_queue = o; o = al256b(o + 256);
-  L.off_slots = o; o = al256b(o + (size_t)grid * 5 * b->dmax * 8);
-  L.off_tri = o; o = al256b(o + (size_t)grid * 6 * (K + 2) * 8);
+  L.off_slots = o; o = al256b(o + (size_t)(grid / cs) * 5 * b->dmax * 8);
+  L.off_tri = o; o = al256b(o + (size_t)grid * 8 * (K + 2) * 8);
   L.off_exps = o; o = al256b(o + (size_t)grid * (K + 2) * 4);
   L.off_coefs = o; o = al256b(o + (size_t)grid * (K + 2) * 8);
   L.total = o;
   return L;
 }
 
-template <int NT>
+static bool valid_config(int threads, int per_sm, int cs) {
+  const bool t_ok = threads == 128 || threads == 256 || threads == 512 || threads == 1024;
+  const bool c_ok = cs == 1 || ((cs == 2 || cs == 4 || cs == 8) && threads >= 512);
+  return t_ok && c_ok && per_sm >= 1 && per_sm <= 16;
+}
+
+template <int NT, int CS>
 static ed_status launch_batch(const ed_batch_s* b, int grid, int K, double tol, int check_every, uint64_t seed,
                               const double* const* starts, int want_vector, const BatchOut& out, const BatchWork& wk,
                               cudaStream_t s) {
-  k_batch_lanczos<NT><<<grid, NT, 0, s>>>(b->d_probs, b->d_order, b->n, K, tol, check_every, seed, starts,
-                                          want_vector, out, wk);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = CS > 1 ? 1 : 0;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, k_batch_lanczos<NT, CS>, (const BatchProblem*)b->d_probs,
+                                           (const int*)b->d_order, b->n, K, tol, check_every, seed, starts, want_vector,
+                                           out, wk);
+  if (e != cudaSuccess) return cuda_fail(e, "k_batch_lanczos");
   ED_CHECK_LAUNCH("k_batch_lanczos");
   return ED_OK;
 }
 
-static ed_status run_batch(const ed_batch_s* b, int threads, int per_sm, int K, double tol, int check_every,
+static ed_status run_batch(const ed_batch_s* b, int threads, int per_sm, int cs, int K, double tol, int check_every,
                            uint64_t seed, const double* const* starts, int want_vector, void* work, size_t bytes,
                            const BatchOut& out, cudaStream_t s) {
-  const int grid = batch_grid(b, per_sm);
-  const BatchLayout L = batch_layout(b, K, grid);
+  if (!valid_config(threads, per_sm, cs))
+    return fail(ED_ERR_INVALID_ARG, "threads 128/256/512/1024; clusters of 2, 4 or 8 CTAs need 512 or 1024 threads");
+  const int grid = batch_grid(b, per_sm, cs);
+  const BatchLayout L = batch_layout(b, K, grid, cs);
   if (!work || bytes < L.total) return fail(ED_ERR_INVALID_ARG, "batch workspace too small (see ed_batch_workspace)");
   char* base = (char*)work;
   BatchWork wk;
@@ -534,23 +648,63 @@ static ed_status run_batch(const ed_batch_s* b, int threads, int per_sm, int K, 
   wk.exps = (int32_t*)(base + L.off_exps);
   wk.coefs = (int64_t*)(base + L.off_coefs);
   ED_CUDA(cudaMemsetAsync(wk.queue, 0, sizeof(int), s));
-  switch (threads) {
-    case 128: return launch_batch<128>(b, grid, K, tol, check_every, seed, starts, want_vector, out, wk, s);
-    case 256: return launch_batch<256>(b, grid, K, tol, check_every, seed, starts, want_vector, out, wk, s);
-    case 512: return launch_batch<512>(b, grid, K, tol, check_every, seed, starts, want_vector, out, wk, s);
-    case 1024: return launch_batch<1024>(b, grid, K, tol, check_every, seed, starts, want_vector, out, wk, s);
-    default: return fail(ED_ERR_INVALID_ARG, "threads must be 128, 256, 512 or 1024");
-  }
+#define ED_BATCH_CASE(NT, CS) \
+  if (threads == NT && cs == CS) return launch_batch<NT, CS>(b, grid, K, tol, check_every, seed, starts, want_vector, out, wk, s);
+  ED_BATCH_CASE(128, 1)
+  ED_BATCH_CASE(256, 1)
+  ED_BATCH_CASE(512, 1)
+  ED_BATCH_CASE(512, 2)
+  ED_BATCH_CASE(512, 4)
+  ED_BATCH_CASE(512, 8)
+  ED_BATCH_CASE(1024, 1)
+  ED_BATCH_CASE(1024, 2)
+  ED_BATCH_CASE(1024, 4)
+  ED_BATCH_CASE(1024, 8)
+#undef ED_BATCH_CASE
+  return fail(ED_ERR_INVALID_ARG, "unsupported launch configuration");
 }
 
-static void default_config(const ed_batch_s* b, int* threads, int* per_sm) {
+// how many clusters of cs CTAs of the NT-thread kernel the device can hold at once (0: none)
+template <int NT, int CS>
+static int clusters_for() {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CS * 16);
+  cfg.blockDim = dim3(NT);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_batch_lanczos<NT, CS>, &cfg) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+static int cluster_schedulable(int threads, int cs) {
+  if (threads == 512 && cs == 2) return clusters_for<512, 2>();
+  if (threads == 512 && cs == 4) return clusters_for<512, 4>();
+  if (threads == 512 && cs == 8) return clusters_for<512, 8>();
+  if (threads == 1024 && cs == 2) return clusters_for<1024, 2>();
+  if (threads == 1024 && cs == 4) return clusters_for<1024, 4>();
+  if (threads == 1024 && cs == 8) return clusters_for<1024, 8>();
+  return 0;
+}
+
+static void default_config(const ed_batch_s* b, int* threads, int* per_sm, int* cs) {
   if (b->tuned_threads) {
     *threads = b->tuned_threads;
     *per_sm = b->tuned_per_sm;
+    *cs = b->tuned_cluster;
     return;
   }
   *threads = 512;
   *per_sm = 2;
+  *cs = 1;
 }
 
 }  // namespace ed
@@ -616,12 +770,15 @@ ED_API ed_status ed_batch_destroy(ed_batch b) {
   return ED_OK;
 }
 
-ED_API ed_status ed_batch_workspace(ed_batch b, int max_steps, int threads, int ctas_per_sm, size_t* bytes) {
+ED_API ed_status ed_batch_workspace(ed_batch b, int max_steps, int threads, int ctas_per_sm, int cluster_size,
+                                    size_t* bytes) {
   if (!b || !bytes) return fail(ED_ERR_INVALID_ARG, "null argument");
   if (max_steps < 1 || max_steps > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
-  int t = threads, ps = ctas_per_sm;
-  if (t <= 0 || ps <= 0) default_config(b, &t, &ps);
-  *bytes = batch_layout(b, max_steps, batch_grid(b, ps)).total;
+  int t = threads, ps = ctas_per_sm, cs = cluster_size;
+  if (t <= 0 || ps <= 0) default_config(b, &t, &ps, &cs);
+  if (cs <= 0) cs = 1;
+  if (!valid_config(t, ps, cs)) return fail(ED_ERR_INVALID_ARG, "unsupported launch configuration");
+  *bytes = batch_layout(b, max_steps, batch_grid(b, ps, cs), cs).total;
   return ED_OK;
 }
 
@@ -629,7 +786,7 @@ ED_API ed_status ed_batch_lanczos(ed_batch b, int max_steps, double tol, int che
                                   const double* const* d_starts, int want_vector, void* d_work, size_t work_bytes,
                                   double* d_alpha, double* d_beta, double* d_energy, double* d_residual,
                                   int32_t* d_steps, double* d_vecs, const int64_t* d_vec_offsets, int threads,
-                                  int ctas_per_sm, ed_stream_t stream) {
+                                  int ctas_per_sm, int cluster_size, ed_stream_t stream) {
   if (!b) return fail(ED_ERR_INVALID_ARG, "null batch");
   if (max_steps < 1 || max_steps > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
   if (!d_alpha || !d_beta || !d_energy || !d_residual || !d_steps)
@@ -638,47 +795,55 @@ ED_API ed_status ed_batch_lanczos(ed_batch b, int max_steps, double tol, int che
   int dev = -1;
   ED_CUDA(cudaGetDevice(&dev));
   if (dev != b->device) return fail(ED_ERR_INVALID_ARG, "batch belongs to another device");
-  int t = threads, ps = ctas_per_sm;
-  if (t <= 0 || ps <= 0) default_config(b, &t, &ps);
+  int t = threads, ps = ctas_per_sm, cs = cluster_size;
+  if (t <= 0 || ps <= 0) default_config(b, &t, &ps, &cs);
+  if (cs <= 0) cs = 1;
   BatchOut out{d_alpha, d_beta, d_energy, d_residual, d_steps, d_vecs, d_vec_offsets};
-  return run_batch(b, t, ps, max_steps, tol, check_every, seed, d_starts, want_vector, d_work, work_bytes, out,
+  return run_batch(b, t, ps, cs, max_steps, tol, check_every, seed, d_starts, want_vector, d_work, work_bytes, out,
                    as_stream(stream));
 }
 
-// Autotuner: times the candidate (threads, CTAs per SM) configurations on a short run
-// (tune_steps Lanczos steps, no vector) and keeps the fastest for this batch.
+// Autotuner: times the candidate (threads, CTAs per SM, cluster size) configurations on a short
+// run (tune_steps Lanczos steps, no vector) and keeps the fastest for this batch. Cluster
+// candidates the device cannot schedule (no active cluster) are skipped.
 ED_API ed_status ed_batch_tune(ed_batch b, int tune_steps, void* d_work, size_t work_bytes, double* d_alpha,
                                double* d_beta, double* d_energy, double* d_residual, int32_t* d_steps,
-                               int* h_threads, int* h_ctas_per_sm, float* h_ms, ed_stream_t stream) {
+                               int* h_threads, int* h_ctas_per_sm, int* h_cluster_size, float* h_ms,
+                               ed_stream_t stream) {
   if (!b) return fail(ED_ERR_INVALID_ARG, "null batch");
   cudaStream_t s = as_stream(stream);
-  const int cand[][2] = {{128, 4}, {256, 2}, {256, 4}, {512, 1}, {512, 2}, {1024, 1}};
+  const int cand[][3] = {{128, 4, 1}, {256, 2, 1},  {256, 4, 1},  {512, 1, 1},  {512, 2, 1},  {1024, 1, 1},
+                         {512, 2, 2}, {1024, 1, 2}, {512, 2, 4},  {1024, 1, 4}, {512, 2, 8},  {1024, 1, 8}};
   float best = 1e30f;
-  int bt = 0, bp = 0;
+  int bt = 0, bp = 0, bc = 0;
   cudaEvent_t e0, e1;
   ED_CUDA(cudaEventCreate(&e0));
   ED_CUDA(cudaEventCreate(&e1));
   BatchOut out{d_alpha, d_beta, d_energy, d_residual, d_steps, nullptr, nullptr};
   for (auto& c : cand) {
-    const size_t need = batch_layout(b, tune_steps, batch_grid(b, c[1])).total;
+    const int grid = batch_grid(b, c[1], c[2]);
+    const size_t need = batch_layout(b, tune_steps, grid, c[2]).total;
     if (need > work_bytes) continue;
+    if (c[2] > 1 && cluster_schedulable(c[0], c[2]) < 1) continue;
     // warm once, then time
-    ED_TRY(run_batch(b, c[0], c[1], tune_steps, 0.0, 0, 1, nullptr, 0, d_work, work_bytes, out, s));
+    ED_TRY(run_batch(b, c[0], c[1], c[2], tune_steps, 0.0, 0, 1, nullptr, 0, d_work, work_bytes, out, s));
     ED_CUDA(cudaEventRecord(e0, s));
-    ED_TRY(run_batch(b, c[0], c[1], tune_steps, 0.0, 0, 1, nullptr, 0, d_work, work_bytes, out, s));
+    ED_TRY(run_batch(b, c[0], c[1], c[2], tune_steps, 0.0, 0, 1, nullptr, 0, d_work, work_bytes, out, s));
     ED_CUDA(cudaEventRecord(e1, s));
     ED_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
     ED_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    if (ms < best) { best = ms; bt = c[0]; bp = c[1]; }
+    if (ms < best) { best = ms; bt = c[0]; bp = c[1]; bc = c[2]; }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (!bt) return fail(ED_ERR_INVALID_ARG, "workspace too small for every tuning candidate");
   b->tuned_threads = bt;
   b->tuned_per_sm = bp;
+  b->tuned_cluster = bc;
   if (h_threads) *h_threads = bt;
   if (h_ctas_per_sm) *h_ctas_per_sm = bp;
+  if (h_cluster_size) *h_cluster_size = bc;
   if (h_ms) *h_ms = best;
   return ED_OK;
 }

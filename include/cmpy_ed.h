@@ -280,7 +280,7 @@ ED_API ed_status ed_batch_destroy(ed_batch batch);
 /* Workspace bytes for max_steps and a launch configuration (threads per CTA in
  * {128,256,512,1024}, CTAs per SM); threads <= 0 uses the tuned (or default) configuration. */
 ED_API ed_status ed_batch_workspace(ed_batch batch, int max_steps, int threads, int ctas_per_sm,
-                                    size_t* h_bytes);
+                                    int cluster_size, size_t* h_bytes);
 /* Ground states of every problem. Outputs (device, problem p): alpha[p*K + k], beta[p*(K+1) + k]
  * (beta[p*(K+1)] = start-vector norm), energy[p], residual[p], steps[p]. d_starts: optional
  * DEVICE array of n device pointers to FP64 start vectors (NULL: seeded uniform(0,1)). With
@@ -291,13 +291,18 @@ ED_API ed_status ed_batch_lanczos(ed_batch batch, int max_steps, double tol, int
                                   void* d_work, size_t work_bytes, double* d_alpha, double* d_beta,
                                   double* d_energy, double* d_residual, int32_t* d_steps,
                                   double* d_vecs, const int64_t* d_vec_offsets, int threads,
-                                  int ctas_per_sm, ed_stream_t stream);
-/* Autotuner: times the candidate launch configurations on a tune_steps run and keeps the
- * fastest for this batch (used when ed_batch_lanczos gets threads <= 0). Synchronous. */
+                                  int ctas_per_sm, int cluster_size, ed_stream_t stream);
+/* Launch configuration: threads per CTA (128, 256, 512, 1024), CTAs per SM, and the
+ * thread-block cluster size per problem (1, or 2/4/8 with 512 or 1024 threads: the cluster's
+ * CTAs share each problem's vectors and exchange their partial sums through distributed
+ * shared memory). threads <= 0 selects the tuned (or default) configuration.
+ * Autotuner: times the candidate configurations on a tune_steps run and keeps the fastest for
+ * this batch (used when ed_batch_lanczos gets threads <= 0). Synchronous. */
 ED_API ed_status ed_batch_tune(ed_batch batch, int tune_steps, void* d_work, size_t work_bytes,
                                double* d_alpha, double* d_beta, double* d_energy,
                                double* d_residual, int32_t* d_steps, int* h_threads,
-                               int* h_ctas_per_sm, float* h_ms, ed_stream_t stream);
+                               int* h_ctas_per_sm, int* h_cluster_size, float* h_ms,
+                               ed_stream_t stream);
 /* Adds the continued fraction of every problem (layout of ed_batch_lanczos, norm^2 =
  * beta[p*(K+1)]^2, shift d_e0[p]) at n_z frequencies into d_g[p*n_z + j] (complex FP64). */
 ED_API ed_status ed_batch_gf_continued_fraction(int n, int max_steps, const double* d_alpha,

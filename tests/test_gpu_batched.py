@@ -75,11 +75,16 @@ def test_batched_vectors_and_configs(cuda):
         assert abs(ei - ref) <= 1e-10 * abs(ref)
         assert abs(torch.linalg.norm(v).item() - 1) < 1e-12
         assert torch.linalg.norm(p.matvec(v) - ei * v).item() < 1e-8 * abs(ei)
-    # every launch configuration gives the same energies
-    for th, ps in ((128, 4), (256, 2), (1024, 1)):
-        b.threads, b.ctas_per_sm = th, ps
-        r2 = b.lanczos(max_steps=300)
+    # every launch configuration gives the same energies, thread-block clusters included
+    # (a cluster of CTAs shares each problem: the partial sums are combined in another order)
+    for th, ps, cs in ((128, 4, 1), (256, 2, 1), (1024, 1, 1), (512, 2, 2), (1024, 1, 4), (512, 2, 8)):
+        b.threads, b.ctas_per_sm, b.cluster_size = th, ps, cs
+        r2 = b.lanczos(max_steps=300, want_vector=cs == 4)
         np.testing.assert_allclose(r2.energy.cpu().numpy(), r1.energy.cpu().numpy(), rtol=1e-12)
+        if cs == 4:
+            for p, ei, v in zip(plans, r2.energy.cpu().numpy(), r2.vectors):
+                assert abs(torch.linalg.norm(v).item() - 1) < 1e-12
+                assert torch.linalg.norm(p.matvec(v) - ei * v).item() < 1e-8 * abs(ei)
 
 
 def test_batched_gf_vs_dense(cuda):
