@@ -408,7 +408,8 @@ def run_disorder_batch(n_real: int = 512, n_freq: int = 1024):
     for m_, s_ in zip(models, sectors):  # plans (setup, untimed)
         for d in (-1, 0, 1):
             m_.plan(s_[0] + d, s_[1])
-    greens_functions_batched(models[:8], sectors[:8], z, gf_levels=levels)  # warm
+    # warm-up on the full set: the launch configurations are tuned (once per batch shape, cached)
+    greens_functions_batched(models, sectors, z, gf_levels=levels)
     (eb, gb), t_batch = _timed(lambda: greens_functions_batched(models, sectors, z, gf_levels=levels))
     n_plain = min(n_real, 64)
 

@@ -24,6 +24,11 @@ __all__ = ["Batch", "BatchResult", "groundstate_all_sectors", "groundstates", "g
            "BatchGraph"]
 
 
+# tuned launch configurations: (device, problem dimensions, tune steps) -> (threads,
+# ctas_per_sm, cluster_size, ms)
+_tune_cache: dict = {}
+
+
 @dataclass
 class BatchResult:
     energy: torch.Tensor      # [n]
@@ -78,7 +83,13 @@ class Batch:
 
     def tune(self, tune_steps: int = 40):
         """Pick threads per CTA, CTAs per SM and the cluster size per problem by timing the
-        candidates; returns (threads, ctas_per_sm, cluster_size, ms)."""
+        candidates; returns (threads, ctas_per_sm, cluster_size, ms). The choice is cached per
+        device and problem-dimension list, so batches of the same shape tune once."""
+        key = (self.device_index, tuple(self.dims), int(tune_steps))
+        hit = _tune_cache.get(key)
+        if hit is not None:
+            self.threads, self.ctas_per_sm, self.cluster_size = hit[:3]
+            return hit
         # size the workspace for the largest candidate grid
         best = 0
         for t, ps, cs in ((128, 4, 1), (256, 2, 1), (256, 4, 1), (512, 1, 1), (512, 2, 1), (1024, 1, 1),
@@ -94,7 +105,8 @@ class Batch:
                                       N.ptr(e), N.ptr(r), N.ptr(s), C.byref(th), C.byref(ps), C.byref(cs),
                                       C.byref(ms), E._stream()))
         self.threads, self.ctas_per_sm, self.cluster_size = int(th.value), int(ps.value), int(cs.value)
-        return self.threads, self.ctas_per_sm, self.cluster_size, float(ms.value)
+        _tune_cache[key] = (self.threads, self.ctas_per_sm, self.cluster_size, float(ms.value))
+        return _tune_cache[key]
 
     def lanczos(self, max_steps: int = 300, tol: float = 1e-12, check_every: int = 10, seed: int = 0,
                 starts: Sequence[torch.Tensor] | None = None, want_vector: bool = False,
