@@ -246,6 +246,9 @@ ED_API ed_status ed_lanczos_workspace(ed_plan plan, const ed_lanczos_params* par
  * Writes alpha[0..steps) and beta[0..steps] (beta[0] = 0, beta[k] couples k-1 and k,
  * beta[steps] is the residual coupling) into d_alpha (FP64[max_steps]) and d_beta
  * (FP64[max_steps+1]), the normalised ground state to d_evec (FP64[D], if want_vector).
+ * The steps are enqueued without waiting; with tol > 0 the host reads the scalars every
+ * check_every steps and tests convergence, and at the end it solves the m x m tridiagonal
+ * eigenproblem (a serial FP64 chain, faster on a host core than in one GPU block).
  * Synchronous at the end (fills *h_result). */
 ED_API ed_status ed_lanczos(ed_plan plan, const ed_lanczos_params* params,
                             const double* d_v0, void* d_work, size_t work_bytes,
