@@ -3,6 +3,7 @@ on a few GB of device memory, not the whole benchmark step).
 
     python -m cmpy_gb300.profile_cases gf14        # Green's-function Lanczos of the 14-site ring
     python -m cmpy_gb300.profile_cases adjoint64   # batched adjoint, 64 SIAMs 1+9, forward + backward
+    python -m cmpy_gb300.profile_cases sweep10     # batched ground states, all 121 sectors, 10-site ring
 
 gf14: the particle-sector Lanczos of the 14-site Hubbard ring (U=4, mu=2, t=1), sector (8,7),
 D = 10,306,296, from a seeded uniform start vector, 12 steps in block fixed point (three
@@ -11,6 +12,10 @@ benchmark step, without its 23.6 GB Krylov store.
 adjoint64: the workload of the benchmark's `adjoint` extra (batched part): 64 SIAMs with
 1 impurity + 9 bath sites, sector (5,5), 1024 Matsubara frequencies at beta=100, seeded bath
 parameters (numpy default_rng(5)), forward and backward once.
+sweep10: the benchmark's `batched_sweep` workload (all 121 sectors of the 10-site Hubbard ring,
+U=6, mu=3, t=1; 300 steps, tol 1e-12, tested every 10 steps) in one batched launch with the
+configuration the tuner picks on GB300 (512 threads, 2 CTAs per SM, clusters of 4 CTAs),
+run twice (the second launch is the one to capture).
 """
 
 from __future__ import annotations
@@ -55,7 +60,23 @@ def adjoint64(n: int = 64) -> None:
     print(f"adjoint64: |grad| = {float(eb.grad.abs().sum() + v.grad.abs().sum()):.6f}")
 
 
-CASES = {"gf14": gf14, "adjoint64": adjoint64}
+def sweep10() -> None:
+    import torch
+
+    from .batched import Batch
+    from .models import ChainLattice, HubbardModel
+
+    m = HubbardModel(ChainLattice(10, True), inter=6.0, mu=3.0, hop=1.0)
+    plans = [m.plan(nu, nd) for nu, nd in m.basis.iter_fillings()]
+    b = Batch(plans)
+    b.threads, b.ctas_per_sm, b.cluster_size = 512, 2, 4
+    for _ in range(2):
+        r = b.lanczos(max_steps=300, tol=1e-12, check_every=10)
+    torch.cuda.synchronize()
+    print(f"sweep10: {len(plans)} sectors, E0 = {float(r.energy.min()):.12f}")
+
+
+CASES = {"gf14": gf14, "adjoint64": adjoint64, "sweep10": sweep10}
 
 if __name__ == "__main__":
     if len(sys.argv) != 2 or sys.argv[1] not in CASES:
