@@ -151,10 +151,34 @@ struct ClusterXch {
   int ph;
 };
 
+// block sum and max together: one shared-memory exchange (same order as bsum / bmax)
+template <int NT>
+__device__ __forceinline__ void bsummax(double& v, unsigned long long& m, BlockScratch<NT>& s) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+    m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) {
+    s.d[w] = v;
+    s.u[w] = m;
+  }
+  __syncthreads();
+  double r = 0.0;
+  unsigned long long q = 0;
+  for (int i = 0; i < NT / 32; ++i) {
+    r += s.d[i];
+    q = max(q, s.u[i]);
+  }
+  v = r;
+  m = q;
+}
+
 template <int NT, int CS>
 __device__ __forceinline__ void cred(double& sumv, unsigned long long& maxv, BlockScratch<NT>& s, ClusterXch& x) {
-  sumv = bsum<NT>(sumv, s);
-  maxv = bmax<NT>(maxv, s);
+  bsummax<NT>(sumv, maxv, s);
   if constexpr (CS > 1) {
     cg::cluster_group cl = cg::this_cluster();
     if (threadIdx.x == 0) {
