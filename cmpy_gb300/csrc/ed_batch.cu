@@ -143,8 +143,9 @@ __device__ __forceinline__ unsigned long long bmax(unsigned long long v, BlockSc
 // Cluster-wide (sum, max) of values held per thread: block totals first, then (CS > 1) the CS
 // block totals through distributed shared memory, in rank order, so every CTA gets the same
 // result. xd / xu: two exchange slots each (alternating with `ph`: a slot is rewritten only
-// after a later cluster barrier, when every CTA has read it). The barrier also orders the
-// global-memory writes of the phase before it for all CTAs of the cluster.
+// after a later cluster barrier, when every CTA has read it). The barrier (release / acquire
+// at cluster scope) also orders the global-memory writes of the phase before it for all CTAs
+// of the cluster.
 struct ClusterXch {
   double* xd;
   unsigned long long* xu;
@@ -185,8 +186,7 @@ __device__ __forceinline__ void cred(double& sumv, unsigned long long& maxv, Blo
       x.xd[x.ph] = sumv;
       x.xu[x.ph] = maxv;
     }
-    __threadfence();
-    cl.sync();
+    cl.sync();  // arrive.release / wait.acquire at cluster scope: orders shared and global writes
     double t = 0.0;
     unsigned long long m = 0;
 #pragma unroll
@@ -204,7 +204,6 @@ __device__ __forceinline__ void cred(double& sumv, unsigned long long& maxv, Blo
 template <int CS>
 __device__ __forceinline__ void csync() {
   if constexpr (CS > 1) {
-    __threadfence();
     cg::this_cluster().sync();
   } else {
     __syncthreads();

@@ -13,8 +13,9 @@ adjoint64: the workload of the benchmark's `adjoint` extra (batched part): 64 SI
 1 impurity + 9 bath sites, sector (5,5), 1024 Matsubara frequencies at beta=100, seeded bath
 parameters (numpy default_rng(5)), forward and backward once.
 sweep10: the benchmark's `batched_sweep` workload (all 121 sectors of the 10-site Hubbard ring,
-U=6, mu=3, t=1; 300 steps, tol 1e-12, tested every 10 steps) in one batched launch with the
-configuration the tuner picks on GB300 (512 threads, 2 CTAs per SM, clusters of 4 CTAs),
+U=6, mu=3, t=1; 300 steps, tol 1e-12, tested every 10 steps) in one batched launch with a
+configuration the tuner picks on GB300 (512 threads, 2 CTAs per SM, clusters of 4 CTAs; its
+other frequent pick, 1024 threads, 1 CTA per SM, clusters of 4, times within a few percent),
 run twice (the second launch is the one to capture).
 """
 
