@@ -590,12 +590,34 @@ __device__ __forceinline__ int64_t shfl64(int64_t v, int src) {
   return (int64_t)__shfl_sync(0xffffffffu, (long long)v, src);
 }
 
+// the bulk copies of one row group (thread 0 of the v3 matvec; kept out of line so that the
+// copy set-up does not take registers from the gather loops)
+template <bool UPW>
+__device__ __noinline__ void mv3_stage(int64_t g, int s, int64_t nu, int64_t nd, int lstride, const int64_t* X,
+                                       const int32_t* up_lst, const int32_t* up_cnt, int64_t* raw, int32_t* lst,
+                                       int32_t* cnt, uint64_t* bar) {
+  const uint64_t keep = policy_evict_last();
+  const int64_t u0 = g * MV3_R;
+  const int nr = (int)min((int64_t)MV3_R, nu - u0);
+  const unsigned row_bytes = (unsigned)(nd * 8);
+  const unsigned lbytes = (unsigned)(MV3_R * lstride * 4), cbytes = (unsigned)(MV3_R * 4 * 4);
+  // order this CTA's earlier generic-proxy reads of the buffers before the async-proxy writes
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  mbar_expect_tx(bar, row_bytes * nr + (UPW ? 0u : lbytes + cbytes));
+  for (int r = 0; r < nr; ++r) bulk_g2s(raw + (size_t)r * nd, X + (u0 + r) * nd, row_bytes, bar, keep);
+  if (!UPW) {
+    bulk_g2s(lst + (size_t)s * MV3_R * lstride, up_lst + u0 * lstride, lbytes, bar, keep);
+    bulk_g2s(cnt + (size_t)s * MV3_R * 4, up_cnt + u0 * 4, cbytes, bar, keep);
+  }
+}
+
 // UPW: the up-neighbour sums were written into W by k_bfp_up_panels (two-pass H·v); the kernel
 // reads them instead of gathering and overwrites W with the result (each element read, then
 // written, by the same thread)
 template <bool DIAG64, bool UPW>
 __global__ void __launch_bounds__(MV3_MAXNT, 1)
     k_bfp_hub_matvec3(BfpHubArgs a, const uint32_t* __restrict__ btab2, int n_b2, int n_b2pos, int max_up,
+                      const int32_t* __restrict__ up_lst, const int32_t* __restrict__ up_cnt,
                       const int64_t* __restrict__ X, int64_t* W, double* partial,
                       unsigned long long* partial_max, BfpState* st, int* status, BfpFuse fz) {
   if (st && *(volatile int*)&st->stop) return;
@@ -615,42 +637,11 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
   const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
   const unsigned row_bytes = (unsigned)(nd * 8);
 
-  // stage group g: its padded up-lists into list buffer s (element offsets of neighbour rows;
-  // padding = the target row) and, from thread 0, the bulk copies of its rows into `raw`
+  // stage group g from thread 0: bulk copies of its rows into `raw` and of its precomputed
+  // padded up-lists and counts (rows u0, u0 + 1; row nu is an empty list) into list buffer s.
+  // Everything lands on one mbarrier phase; no other thread waits on global loads here.
   auto stage = [&](int64_t g, int s) {
-    const int64_t u0 = g * MV3_R;
-    const int nr = (int)min((int64_t)MV3_R, nu - u0);
-    for (int t = tid; t < (UPW ? 0 : MV3_R * L.lstride); t += nt) {
-      const int r = t / L.lstride, e = t - r * L.lstride;
-      if (r >= nr) continue;
-      const int64_t u = u0 + r;
-      const int32_t o0 = __ldg(a.up_off + u), n = __ldg(a.up_off + u + 1) - o0, np = __ldg(a.up_npos + u);
-      const int32_t cp = (np + 3) & ~3, cn = ((n - np) + 3) & ~3;
-      int32_t v = (int32_t)(u * nd);
-      if (e < cp) {
-        if (e < np) v = __ldg(a.up_idx + o0 + e) * (int32_t)nd;
-      } else if (e < cp + cn) {
-        if (e - cp < n - np) v = __ldg(a.up_idx + o0 + np + (e - cp)) * (int32_t)nd;
-      }
-      lst[(s * MV3_R + r) * L.lstride + e] = v;
-    }
-    for (int r = tid; r < MV3_R; r += nt) {
-      int32_t cp = 0, cn = 0, corr = 0;
-      if (r < nr) {
-        const int64_t u = u0 + r;
-        const int32_t n = __ldg(a.up_off + u + 1) - __ldg(a.up_off + u), np = __ldg(a.up_npos + u);
-        cp = (np + 3) & ~3;
-        cn = ((n - np) + 3) & ~3;
-        corr = (cn - (n - np)) - (cp - np);  // padding copies of the target row, with sign
-      }
-      cnt[(s * MV3_R + r) * 4 + 0] = cp;
-      cnt[(s * MV3_R + r) * 4 + 1] = cn;
-      cnt[(s * MV3_R + r) * 4 + 2] = corr;
-    }
-    if (tid == 0) {
-      mbar_expect_tx(bar, row_bytes * nr);
-      for (int r = 0; r < nr; ++r) bulk_g2s(raw + (size_t)r * nd, X + (u0 + r) * nd, row_bytes, bar, keep);
-    }
+    if (tid == 0) mv3_stage<UPW>(g, s, nu, nd, L.lstride, X, up_lst, up_cnt, raw, lst, cnt, bar);
   };
 
   // one-time set-up: the table, the zero slot pair, the barrier
@@ -1238,6 +1229,27 @@ ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
   B.n_b2 = n_rows / 2;
   B.n_b2pos = pos_pad / 2;
   B.max_up = max_up;
+  {
+    // staged up lists of the v3 matvec (element offsets must fit int32: checked at variant
+    // selection, dim < 2^31)
+    const int ls = mv3_layout(nd, B.n_b2, max_up).lstride;
+    std::vector<int32_t> lst((size_t)(nu + 1) * ls, 0), cnt((size_t)(nu + 1) * 4, 0);
+    for (int64_t r = 0; r < nu; ++r) {
+      const int32_t o0 = boff[r], n = boff[r + 1] - o0, np = bnpos[r];
+      const int32_t cp = (np + 3) & ~3, cn = ((n - np) + 3) & ~3;
+      const int32_t self = (int32_t)(r * nd);
+      int32_t* L = lst.data() + (size_t)r * ls;
+      for (int e = 0; e < ls; ++e) L[e] = self;
+      for (int e = 0; e < np; ++e) L[e] = (int32_t)((int64_t)bidx[o0 + e] * nd);
+      for (int e = 0; e < n - np; ++e) L[cp + e] = (int32_t)((int64_t)bidx[o0 + np + e] * nd);
+      cnt[(size_t)r * 4 + 0] = cp;
+      cnt[(size_t)r * 4 + 1] = cn;
+      cnt[(size_t)r * 4 + 2] = (cn - (n - np)) - (cp - np);  // padding copies of the row, with sign
+    }
+    ED_TRY(up(&B.up_lst, lst.data(), lst.size() * 4));
+    ED_TRY(up(&B.up_cnt, cnt.data(), cnt.size() * 4));
+    B.up_lstride = ls;
+  }
   if (!diag64) {
     ED_TRY(up(&B.e_up_int, eui.data(), eui.size() * 4));
     ED_TRY(up(&B.e_dn_int, edi.data(), edi.size() * 4));
@@ -1253,6 +1265,7 @@ ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
 void free_bfp(ed_plan_s* p) {
   BfpTables& B = p->bfp;
   cudaFree(B.up_off); cudaFree(B.up_npos); cudaFree(B.up_idx); cudaFree(B.dn_tab); cudaFree(B.dn_btab2);
+  cudaFree(B.up_lst); cudaFree(B.up_cnt);
   cudaFree(B.e_up_int); cudaFree(B.e_dn_int); cudaFree(B.e_up_fx); cudaFree(B.e_dn_fx);
   B = BfpTables();
 }
@@ -1307,7 +1320,8 @@ static int matvec_variant(const ed_plan_s* p) {
   const bool v2_ok = p->bfp.vec2 && v2_smem(p) + MV2_STATIC_SMEM <= optin && p->num_up >= 1;
   // list entries are int32 element offsets u * nd: the vector must have fewer than 2^31 elements
   // (and the table holds 16-bit byte offsets: nd < 4096)
-  const bool v3_ok = p->bfp.vec2 && p->bfp.dn_btab2 && v3_smem(p) + MV3_STATIC_SMEM <= optin && p->num_up >= 1 &&
+  const bool v3_ok = p->bfp.vec2 && p->bfp.dn_btab2 && p->bfp.up_lst && v3_smem(p) + MV3_STATIC_SMEM <= optin &&
+                     p->num_up >= 1 &&
                      p->dim < ((int64_t)1 << 31) && p->num_dn < 4096;
   // two-pass (4): column panels of 4 (nd % 4 == 0), a panel of all rows in half the shared memory
   const bool v4_ok = v3_ok && p->num_dn % MV_PW == 0 && (size_t)p->num_up * MV_PW * 8 + 1024 <= optin / 2;
@@ -1372,8 +1386,8 @@ static ed_status launch_v3(const ed_plan_s* p, int g, const int64_t* X, int64_t*
     ED_CHECK_LAUNCH("k_bfp_up_panels");
   }
   k_bfp_hub_matvec3<DIAG64, UPW><<<g, v3_threads(p), v3_smem(p), s>>>(bfp_args(p), B.dn_btab2, B.n_b2, B.n_b2pos,
-                                                                      B.max_up, X, W, partial, partial_max, st,
-                                                                      status, fz);
+                                                                      B.max_up, B.up_lst, B.up_cnt, X, W, partial,
+                                                                      partial_max, st, status, fz);
   ED_CHECK_LAUNCH("k_bfp_hub_matvec3");
   return ED_OK;
 }

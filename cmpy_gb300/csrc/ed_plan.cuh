@@ -69,6 +69,13 @@ struct BfpTables {
   uint32_t* dn_btab2 = nullptr;
   int n_b2 = 0, n_b2pos = 0;
   int max_up = 0;               // most up-neighbours of one row
+  // up lists as the v3 matvec stages them, one bulk copy per row group: [nu + 1][up_lstride]
+  // element offsets idx * nd (+ segment, then - segment, each padded to a multiple of 4 with
+  // the row's own offset), and [nu + 1][4] = (+ length, - length, padding correction, 0);
+  // row nu is an empty list (read by the second row slot of a final one-row group)
+  int32_t* up_lst = nullptr;
+  int32_t* up_cnt = nullptr;
+  int up_lstride = 0;
   int32_t* e_up_int = nullptr;  // [nu]
   int32_t* e_dn_int = nullptr;  // [nd]
 };

@@ -70,7 +70,9 @@ def test_fixed_random_eps(cuda, nu, nd):
 
 @pytest.mark.parametrize("case", [("chain6", 6, False, 3, 3, 4.0, 2.0, 1.0), ("ring8", 8, True, 4, 3, 6.0, 3.0, 1.0),
                                   ("ring8h", 8, True, 4, 4, 3.0, 1.5, 0.5), ("ring9odd", 9, True, 4, 5, 4.0, 2.0, 1.0),
-                                  ("ring10", 10, True, 5, 5, 6.0, 3.0, -1.0)])
+                                  ("ring10", 10, True, 5, 5, 6.0, 3.0, -1.0),
+                                  # odd number of up rows (165): the last row group holds one row
+                                  ("ring11odd", 11, True, 3, 4, 4.0, 2.0, 1.0)])
 def test_matvec_fixed_bit_exact(cuda, case):
     from cmpy_gb300 import engine as E
 
