@@ -133,6 +133,7 @@ _SIGNATURES = {
     "ed_coo_hopping": (I32, [P, I64, P, I64, I32, I32, I32, F64, P, P, P, I64, C.POINTER(I64), P]),
     "ed_coo_plan": (I32, [PLAN, P, P, P, I64, C.POINTER(I64), P]),
     "ed_apply_fermion": (I32, [PLAN, PLAN, I32, I32, I32, I32, P, P, I64, I64, I64, P]),
+    "ed_apply_fermion_batch": (I32, [P, P, I32, I32, I32, I32, I32, P, P, P, P, P]),
     "ed_lanczos_workspace": (I32, [PLAN, C.POINTER(LanczosParams), C.POINTER(C.c_size_t)]),
     "ed_lanczos": (
         I32,

@@ -182,22 +182,31 @@ def greens_functions_batched(models, sectors, z, pos: int = 0, sigma: int = 1, g
     sector: batched ground states with vectors, c^dag / c on every ground state, batched
     Lanczos coefficients in the neighbouring sectors and a batched continued fraction.
     Returns (energies [n], G [n, nz])."""
-    plans = [m.plan(*s) for m, s in zip(models, sectors)]
-    gs, _ = groundstates(plans, gs_steps, tol, 10, True, tune)
+    # the ground-state sector and its two neighbours of every model, from one descriptor each
+    trip = []
+    for m, (nu, nd) in zip(models, sectors):
+        want = [(nu, nd)]
+        for delta in (1, -1):
+            tu, td = (nu + delta, nd) if sigma == 1 else (nu, nd + delta)
+            want.append((tu, td) if (0 <= tu <= m.num_sites and 0 <= td <= m.num_sites) else None)
+        trip.append(m.plans(want))
+    plans = [t[0] for t in trip]
+    gs, gb = groundstates(plans, gs_steps, tol, 10, True, tune)
+    # host offsets of the ground states in the batch's vector buffer
+    gs_off = np.zeros(len(plans), dtype=np.int64)
+    if len(plans) > 1:
+        gs_off[1:] = np.cumsum(gb.dims)[:-1]
     zt = E._as_dev_c128(z)
     g = torch.zeros((len(plans), zt.numel()), dtype=torch.complex128, device=zt.device)
-    for delta, create, sign in ((1, True, 1), (-1, False, -1)):
-        tplans, starts, idx = [], [], []
-        for i, (m, (nu, nd)) in enumerate(zip(models, sectors)):
-            tu, td = (nu + delta, nd) if sigma == 1 else (nu, nd + delta)
-            if not (0 <= tu <= m.num_sites and 0 <= td <= m.num_sites):
-                continue
-            tp = m.plan(tu, td)
-            tplans.append(tp)
-            starts.append(plans[i].apply_fermion(tp, pos, sigma, create, gs.vectors[i]))
-            idx.append(i)
+    for slot, (delta, create, sign) in enumerate(((1, True, 1), (-1, False, -1)), start=1):
+        idx = [i for i, t in enumerate(trip) if t[slot] is not None]
+        tplans = [trip[i][slot] for i in idx]
         if not tplans:
             continue
+        # c^dag / c on every ground state in one native call
+        ybuf, y_off = E.apply_fermion_batch([plans[i] for i in idx], tplans, pos, sigma, create, gb._vbuf,
+                                            gs_off[idx])
+        starts = [ybuf[o:o + t.dim] for o, t in zip(y_off.tolist(), tplans)]
         b = Batch(tplans)
         if tune:
             b.tune(min(40, gf_levels))

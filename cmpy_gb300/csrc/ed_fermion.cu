@@ -70,9 +70,8 @@ using namespace ed;
 
 extern "C" {
 
-ED_API ed_status ed_apply_fermion(ed_plan p, ed_plan pt, int pos, int sigma, int create, int jw_sign,
-                                  const double* d_x, double* d_y, int64_t nvec, int64_t ldx, int64_t ldy,
-                                  ed_stream_t stream) {
+// argument checks shared by the single and the batched entry point
+static ed_status check_fermion_pair(const ed_plan_s* p, const ed_plan_s* pt, int pos, int sigma, int create) {
   ED_TRY(check_plan(p));
   ED_TRY(check_plan(pt));
   if (p->kind != 0 || pt->kind != 0) return fail(ED_ERR_INVALID_ARG, "fermion operators need fermionic plans");
@@ -84,10 +83,11 @@ ED_API ed_status ed_apply_fermion(ed_plan p, ed_plan pt, int pos, int sigma, int
     return fail(ED_ERR_INVALID_ARG, "target plan is not the neighbouring up sector");
   if (sigma == 2 && (pt->n_dn != p->n_dn + dn_ || pt->n_up != p->n_up))
     return fail(ED_ERR_INVALID_ARG, "target plan is not the neighbouring dn sector");
-  if (nvec < 0 || ldx < p->dim || ldy < pt->dim) return fail(ED_ERR_INVALID_ARG, "bad n_vec / leading dimensions");
-  if (pt->dim == 0 || nvec == 0) return ED_OK;
-  if (!d_x || !d_y) return fail(ED_ERR_INVALID_ARG, "null vector");
-  cudaStream_t s = as_stream(stream);
+  return ED_OK;
+}
+
+static void launch_fermion(const ed_plan_s* p, const ed_plan_s* pt, int pos, int sigma, int create, int jw_sign,
+                           const double* d_x, double* d_y, int64_t nvec, int64_t ldx, int64_t ldy, cudaStream_t s) {
   const int sms = p->ctx->num_sms;
   const int g = (int)std::min<int64_t>(pt->num_up * nvec, (int64_t)sms * 16);
   if (sigma == 1) {
@@ -97,7 +97,42 @@ ED_API ed_status ed_apply_fermion(ed_plan p, ed_plan pt, int pos, int sigma, int
     k_fermion_dn<<<g, 256, 0, s>>>(p->ctx->d_binom, pt->up.states, pt->dn.states, pt->num_up, p->num_dn, pt->num_dn,
                                    pos, create, jw_sign, d_x, d_y, nvec, ldx, ldy);
   }
+}
+
+ED_API ed_status ed_apply_fermion(ed_plan p, ed_plan pt, int pos, int sigma, int create, int jw_sign,
+                                  const double* d_x, double* d_y, int64_t nvec, int64_t ldx, int64_t ldy,
+                                  ed_stream_t stream) {
+  ED_TRY(check_fermion_pair(p, pt, pos, sigma, create));
+  if (nvec < 0 || ldx < p->dim || ldy < pt->dim) return fail(ED_ERR_INVALID_ARG, "bad n_vec / leading dimensions");
+  if (pt->dim == 0 || nvec == 0) return ED_OK;
+  if (!d_x || !d_y) return fail(ED_ERR_INVALID_ARG, "null vector");
+  launch_fermion(p, pt, pos, sigma, create, jw_sign, d_x, d_y, nvec, ldx, ldy, as_stream(stream));
   ED_CHECK_LAUNCH("ed_apply_fermion");
+  return ED_OK;
+}
+
+ED_API ed_status ed_apply_fermion_batch(const ed_plan* plans, const ed_plan* targets, int n, int pos, int sigma,
+                                        int create, int jw_sign, const double* d_x, const int64_t* x_off,
+                                        double* d_y, const int64_t* y_off, ed_stream_t stream) {
+  if (n < 0) return fail(ED_ERR_INVALID_ARG, "negative problem count");
+  if (n == 0) return ED_OK;
+  if (!plans || !targets || !x_off || !y_off) return fail(ED_ERR_INVALID_ARG, "null plan or offset array");
+  if (!d_x || !d_y) return fail(ED_ERR_INVALID_ARG, "null vector");
+  // every problem is checked before the first launch: an error leaves d_y untouched
+  for (int i = 0; i < n; ++i) {
+    ED_TRY(check_fermion_pair(plans[i], targets[i], pos, sigma, create));
+    if (x_off[i] < 0 || y_off[i] < 0) return fail(ED_ERR_INVALID_ARG, "negative vector offset");
+  }
+  const cudaStream_t s = as_stream(stream);
+  int launched = 0;
+  for (int i = 0; i < n; ++i) {
+    const ed_plan_s* p = plans[i];
+    const ed_plan_s* pt = targets[i];
+    if (pt->dim == 0) continue;
+    launch_fermion(p, pt, pos, sigma, create, jw_sign, d_x + x_off[i], d_y + y_off[i], 1, p->dim, pt->dim, s);
+    ++launched;
+  }
+  ED_CHECK_LAUNCH_N("ed_apply_fermion_batch", launched);
   return ED_OK;
 }
 

@@ -275,6 +275,34 @@ class Plan:
             return Y.reshape(-1) if vec else Y.t()
 
 
+def apply_fermion_batch(plans, targets, pos: int, sigma: int, create: bool, x: torch.Tensor, x_offsets,
+                        jw_sign: bool = False):
+    """c^dag (create) or c on site pos, spin sigma, for many problems in one native call:
+    problem i maps x[x_offsets[i] : x_offsets[i] + plans[i].dim] into its target sector.
+    Returns (y, y_offsets): one buffer holding every target vector, problem i at
+    y[y_offsets[i] : y_offsets[i] + targets[i].dim]."""
+    n = len(plans)
+    if len(targets) != n or len(x_offsets) != n:
+        raise ValueError("plans, targets and x_offsets must have the same length")
+    dims = np.array([t.dim for t in targets], dtype=np.int64)
+    y_off = np.zeros(n, dtype=np.int64)
+    if n > 1:
+        y_off[1:] = np.cumsum(dims)[:-1]
+    y = torch.empty(int(dims.sum()), dtype=torch.float64, device=device())
+    if n == 0:
+        return y, y_off
+    xo = np.ascontiguousarray(x_offsets, dtype=np.int64)
+    x = _as_dev_f64(x).reshape(-1)
+    if np.any(xo + np.array([p.dim for p in plans], dtype=np.int64) > x.numel()):
+        raise ValueError("a source vector runs past the end of x")
+    arr_p = (C.c_void_p * n)(*[p.handle.value for p in plans])
+    arr_t = (C.c_void_p * n)(*[t.handle.value for t in targets])
+    N.check(N.lib().ed_apply_fermion_batch(arr_p, arr_t, n, int(pos), int(sigma), int(bool(create)),
+                                           int(bool(jw_sign)), N.ptr(x), xo.ctypes.data, N.ptr(y),
+                                           y_off.ctypes.data, _stream()))
+    return y, y_off
+
+
 _basis_plans: dict = {}
 _basis_lock = threading.Lock()
 

@@ -186,13 +186,26 @@ class AbstractManyBodyModel(AbstractModel):
         return None
 
     def plan(self, n_up: int, n_dn: int) -> "E.Plan":
+        return self.plans([(n_up, n_dn)])[0]
+
+    def plans(self, sectors) -> list:
+        """Plans of several (n_up, n_dn) sectors of the current parameters (one descriptor for
+        all of them); a None entry gives None."""
         desc = self.fermion_descriptor()
         if desc is None:
             raise NotImplementedError(f"{type(self).__name__} has no engine descriptor")
         eps, u, bonds, width = desc
-        key = (tuple(np.asarray(eps, float).tolist()), tuple(np.asarray(u, float).tolist()),
-               tuple(tuple(b) for b in bonds), int(width), int(n_up), int(n_dn))
-        return self._plans.get(key, lambda: E.Plan.fermion(self.num_sites, eps, u, bonds, n_up, n_dn, width))
+        base = (tuple(np.asarray(eps, float).tolist()), tuple(np.asarray(u, float).tolist()),
+                tuple(tuple(b) for b in bonds), int(width))
+        out = []
+        for sec in sectors:
+            if sec is None:
+                out.append(None)
+                continue
+            nu, nd = int(sec[0]), int(sec[1])
+            out.append(self._plans.get(base + (nu, nd),
+                                       lambda nu=nu, nd=nd: E.Plan.fermion(self.num_sites, eps, u, bonds, nu, nd, width)))
+        return out
 
     # -- reference surface -----------------------------------------------------------------
     @abstractmethod

@@ -214,6 +214,16 @@ ED_API ed_status ed_apply_fermion(ed_plan plan, ed_plan plan_target, int pos, in
                                   int64_t n_vec, int64_t ld_x, int64_t ld_y,
                                   ed_stream_t stream);
 
+/* The same operator on n independent problems in one call (no reference counterpart; the
+ * batched Green's-function driver applies c^dag / c to every realisation's ground state):
+ * problem i maps d_x + x_off[i] (plans[i]->dim values) to d_y + y_off[i] (targets[i]->dim
+ * values). x_off / y_off are HOST arrays of element offsets. Every problem is checked (as in
+ * ed_apply_fermion) before the first launch, so an error leaves d_y untouched. */
+ED_API ed_status ed_apply_fermion_batch(const ed_plan* plans, const ed_plan* targets, int n,
+                                        int pos, int sigma, int create, int jw_sign,
+                                        const double* d_x, const int64_t* x_off, double* d_y,
+                                        const int64_t* y_off, ed_stream_t stream);
+
 /* ---- Lanczos ground state (replaces eigsh in cmpy/exactdiag.py:24-43) ----------------- */
 
 typedef struct ed_lanczos_params {

@@ -140,3 +140,37 @@ def test_batch_rejects_non_fixed_point(cuda):
     s = SingleImpurityAndersonModel(u=4.0, eps_bath=[-1.3, 0.7], v=[0.31, 0.2])
     with pytest.raises(ValueError):
         Batch([s.plan(1, 1)])
+
+
+@pytest.mark.parametrize("sigma,create,jw", [(1, True, False), (1, False, True), (2, True, True), (2, False, False)])
+def test_apply_fermion_batch_equals_single(cuda, sigma, create, jw):
+    """ed_apply_fermion_batch: every problem bit-identical to its own ed_apply_fermion call."""
+    from cmpy_gb300 import engine as E
+
+    rng = np.random.default_rng(11)
+    models = [_hub(7, True, inter=3.0, eps=rng.uniform(-1, 1, 7), mu=1.5) for _ in range(5)]
+    sectors = [(3, 3), (2, 4), (4, 2), (1, 3), (3, 1)]
+    d = 1 if create else -1
+    src, dst = [], []
+    for m, (nu, nd) in zip(models, sectors):
+        src.append(m.plan(nu, nd))
+        dst.append(m.plan(nu + d, nd) if sigma == 1 else m.plan(nu, nd + d))
+    x_off = np.concatenate([[0], np.cumsum([p.dim for p in src])[:-1]]).astype(np.int64)
+    x = torch.randn(int(sum(p.dim for p in src)) + 3, dtype=torch.float64, device="cuda")
+    y, y_off = E.apply_fermion_batch(src, dst, 2, sigma, create, x, x_off, jw_sign=jw)
+    for p, t, xo, yo in zip(src, dst, x_off, y_off):
+        ref = p.apply_fermion(t, 2, sigma, create, x[xo:xo + p.dim], jw_sign=jw)
+        assert torch.equal(y[yo:yo + t.dim], ref)
+
+
+def test_apply_fermion_batch_rejects_before_launch(cuda):
+    from cmpy_gb300 import engine as E
+
+    m = _hub(6, False, inter=4.0, mu=2.0)
+    src = [m.plan(3, 3), m.plan(2, 3)]
+    dst = [m.plan(4, 3), m.plan(2, 4)]  # second target is not the up-neighbour sector
+    x = torch.zeros(src[0].dim + src[1].dim, dtype=torch.float64, device="cuda")
+    with pytest.raises(Exception):
+        E.apply_fermion_batch(src, dst, 0, 1, True, x, [0, src[0].dim])
+    with pytest.raises(ValueError):
+        E.apply_fermion_batch(src, [m.plan(4, 3), m.plan(3, 3)], 0, 1, True, x, [0, src[0].dim + 1])
