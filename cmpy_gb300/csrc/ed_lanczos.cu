@@ -127,32 +127,77 @@ __global__ void k_lz_update(double* __restrict__ w, const double* __restrict__ q
 
 // ---- full reorthogonalisation: classical Gram-Schmidt against Q[0..m) -----------------------
 // h = Q^T w. Block b owns the element chunk [b*ch, (b+1)*ch) (ch = ceil(n / gridDim)); each warp
-// forms whole dot products of that chunk with vectors j = warp, warp + nwarps, ... (four FMA
-// chains per lane, shuffle reduction), partial[j*gridDim + b]; the last block to finish sums
-// the partials of every j in block order. No block-wide barrier per vector.
-__global__ void k_multidot(const double* __restrict__ Q, int64_t ldq, int m, const double* __restrict__ w, int64_t n,
-                           double* partial, double* h, LzState* st) {
+// forms whole dot products of that chunk with vectors j = warp, warp + nwarps, ... and walks the
+// chunk in tiles of RD_TILE elements: each lane issues its RD_EPL loads of q_j and of w (w hits
+// L1 after the first vector) before the FMAs, so a warp keeps 2*RD_EPL loads in flight (the
+// Krylov store streams from HBM; with few loads in flight the kernel waits on latency, not on
+// the FP64 pipe). Four FMA chains per lane, shuffle reduction, partial[j*gridDim + b]; the last
+// block to finish sums the partials of every j in block order. No block-wide barrier per vector.
+constexpr int RD_EPL = 16;
+constexpr int RD_TILE = 32 * RD_EPL;
+__global__ void __launch_bounds__(LZ_NT) k_multidot(const double* __restrict__ Q, int64_t ldq, int m,
+                                                    const double* __restrict__ w, int64_t n, double* partial,
+                                                    double* h, LzState* st) {
   if (lz_stopped(st)) return;
   const int64_t ch = (n + gridDim.x - 1) / gridDim.x;
   const int64_t i0 = (int64_t)blockIdx.x * ch;
-  const int64_t len = max((int64_t)0, min(n, i0 + ch) - i0);
+  const int64_t i1 = min(n, i0 + ch);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const double* wc = w + i0;
-  for (int j = warp; j < m; j += nw) {
-    const double* q = Q + (int64_t)j * ldq + i0;
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    int64_t i = lane;
-    for (; i + 96 < len; i += 128) {
-      a0 = fma(__ldg(q + i), __ldg(wc + i), a0);
-      a1 = fma(__ldg(q + i + 32), __ldg(wc + i + 32), a1);
-      a2 = fma(__ldg(q + i + 64), __ldg(wc + i + 64), a2);
-      a3 = fma(__ldg(q + i + 96), __ldg(wc + i + 96), a3);
+  if (i1 - i0 <= RD_TILE) {
+    // one tile per block: w stays in registers for every vector (one load per FMA)
+    double wr[RD_EPL];
+#pragma unroll
+    for (int e = 0; e < RD_EPL; ++e) {
+      const int64_t i = i0 + lane + 32 * e;
+      wr[e] = i < i1 ? __ldg(w + i) : 0.0;
     }
-    for (; i < len; i += 32) a0 = fma(__ldg(q + i), __ldg(wc + i), a0);
+    for (int j = warp; j < m; j += nw) {
+      const double* q = Q + (int64_t)j * ldq;
+      double qv[RD_EPL];
+#pragma unroll
+      for (int e = 0; e < RD_EPL; ++e) {
+        const int64_t i = i0 + lane + 32 * e;
+        qv[e] = i < i1 ? __ldg(q + i) : 0.0;
+      }
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+#pragma unroll
+      for (int e = 0; e < RD_EPL; e += 4) {
+        a0 = fma(qv[e], wr[e], a0);
+        a1 = fma(qv[e + 1], wr[e + 1], a1);
+        a2 = fma(qv[e + 2], wr[e + 2], a2);
+        a3 = fma(qv[e + 3], wr[e + 3], a3);
+      }
+      double acc = (a0 + a1) + (a2 + a3);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) partial[(int64_t)j * gridDim.x + blockIdx.x] = acc;
+    }
+  } else {
+  for (int j = warp; j < m; j += nw) {
+    const double* q = Q + (int64_t)j * ldq;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    for (int64_t t0 = i0; t0 < i1; t0 += RD_TILE) {
+      double qv[RD_EPL], wv[RD_EPL];
+#pragma unroll
+      for (int e = 0; e < RD_EPL; ++e) {
+        const int64_t i = t0 + lane + 32 * e;
+        const bool ok = i < i1;
+        qv[e] = ok ? __ldg(q + i) : 0.0;
+        wv[e] = ok ? __ldg(w + i) : 0.0;
+      }
+#pragma unroll
+      for (int e = 0; e < RD_EPL; e += 4) {
+        a0 = fma(qv[e], wv[e], a0);
+        a1 = fma(qv[e + 1], wv[e + 1], a1);
+        a2 = fma(qv[e + 2], wv[e + 2], a2);
+        a3 = fma(qv[e + 3], wv[e + 3], a3);
+      }
+    }
     double acc = (a0 + a1) + (a2 + a3);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) partial[(int64_t)j * gridDim.x + blockIdx.x] = acc;
+  }
   }
   if (last_block(&st->ticket[2])) {
     for (int j = warp; j < m; j += nw) {
@@ -166,31 +211,62 @@ __global__ void k_multidot(const double* __restrict__ Q, int64_t ldq, int m, con
   }
 }
 
-// w -= sum_j h[j] Q[j] (four independent FMA chains per element); optionally accumulates ||w||^2
-// and finalises beta_{k+1}. m <= RO_MAX (checked by the host).
+// w -= sum_j h[j] Q[j]; optionally accumulates ||w||^2 and finalises beta_{k+1}. Each thread owns
+// two elements per grid-stride step (i and i + LZ_NT, each coalesced across the warp), so one
+// shared-memory read of h_j serves two FMAs, and walks j in groups of RA_J: the 2*RA_J loads of a
+// group are issued before their FMAs (four chains per element). m <= RO_MAX (checked by the host).
 constexpr int RO_MAX = 1024;
-__global__ void k_multiaxpy(const double* __restrict__ Q, int64_t ldq, int m, const double* __restrict__ h,
-                            double* __restrict__ w, int64_t n, double* partial, LzState* st, double* beta_next,
-                            int k, int final_norm, const double* alpha_k) {
+constexpr int RA_J = 8;
+__global__ void __launch_bounds__(LZ_NT, 3) k_multiaxpy(const double* __restrict__ Q, int64_t ldq, int m,
+                                                     const double* __restrict__ h, double* __restrict__ w, int64_t n,
+                                                     double* partial, LzState* st, double* beta_next, int k,
+                                                     int final_norm, const double* alpha_k) {
   if (lz_stopped(st)) return;
   __shared__ double sm[LZ_NT / 32];
-  __shared__ double hs[RO_MAX];
-  for (int j = threadIdx.x; j < m; j += LZ_NT) hs[j] = h[j];
+  __shared__ double hs[RO_MAX + RA_J];
+  for (int j = threadIdx.x; j < m + RA_J; j += LZ_NT) hs[j] = j < m ? h[j] : 0.0;
   __syncthreads();
   double v = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)LZ_NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * LZ_NT) {
-    double x0 = w[i], x1 = 0.0, x2 = 0.0, x3 = 0.0;
-    int j = 0;
-    for (; j + 3 < m; j += 4) {
-      x0 = fma(-hs[j], __ldg(Q + (int64_t)j * ldq + i), x0);
-      x1 = fma(-hs[j + 1], __ldg(Q + (int64_t)(j + 1) * ldq + i), x1);
-      x2 = fma(-hs[j + 2], __ldg(Q + (int64_t)(j + 2) * ldq + i), x2);
-      x3 = fma(-hs[j + 3], __ldg(Q + (int64_t)(j + 3) * ldq + i), x3);
+  const int mf = m - m % RA_J;  // vectors in full groups
+  const int64_t step = (int64_t)gridDim.x * 2 * LZ_NT;
+  for (int64_t ia = blockIdx.x * (int64_t)(2 * LZ_NT) + threadIdx.x; ia < n; ia += step) {
+    const int64_t ib = ia + LZ_NT;
+    const bool hb = ib < n;
+    const int64_t ibc = hb ? ib : ia;  // a valid address for the second element's loads
+    double xa0 = w[ia], xa1 = 0.0, xa2 = 0.0, xa3 = 0.0;
+    double xb0 = hb ? w[ib] : 0.0, xb1 = 0.0, xb2 = 0.0, xb3 = 0.0;
+    for (int j = 0; j < mf; j += RA_J) {
+      double qa[RA_J], qb[RA_J];
+#pragma unroll
+      for (int e = 0; e < RA_J; ++e) {
+        qa[e] = __ldg(Q + (int64_t)(j + e) * ldq + ia);
+        qb[e] = __ldg(Q + (int64_t)(j + e) * ldq + ibc);
+      }
+#pragma unroll
+      for (int e = 0; e < RA_J; e += 4) {
+        const double h0 = -hs[j + e], h1 = -hs[j + e + 1], h2 = -hs[j + e + 2], h3 = -hs[j + e + 3];
+        xa0 = fma(h0, qa[e], xa0);
+        xa1 = fma(h1, qa[e + 1], xa1);
+        xa2 = fma(h2, qa[e + 2], xa2);
+        xa3 = fma(h3, qa[e + 3], xa3);
+        xb0 = fma(h0, qb[e], xb0);
+        xb1 = fma(h1, qb[e + 1], xb1);
+        xb2 = fma(h2, qb[e + 2], xb2);
+        xb3 = fma(h3, qb[e + 3], xb3);
+      }
     }
-    for (; j < m; ++j) x0 = fma(-hs[j], __ldg(Q + (int64_t)j * ldq + i), x0);
-    const double x = (x0 + x1) + (x2 + x3);
-    w[i] = x;
-    v = fma(x, x, v);
+    for (int j = mf; j < m; ++j) {
+      xa0 = fma(-hs[j], __ldg(Q + (int64_t)j * ldq + ia), xa0);
+      xb0 = fma(-hs[j], __ldg(Q + (int64_t)j * ldq + ibc), xb0);
+    }
+    const double xa = (xa0 + xa1) + (xa2 + xa3);
+    w[ia] = xa;
+    v = fma(xa, xa, v);
+    if (hb) {
+      const double xb = (xb0 + xb1) + (xb2 + xb3);
+      w[ib] = xb;
+      v = fma(xb, xb, v);
+    }
   }
   v = block_sum<LZ_NT>(v, sm);
   if (threadIdx.x == 0) partial[blockIdx.x] = v;
@@ -355,8 +431,9 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
   ED_CUDA(cudaMemsetAsync(d_beta, 0, (K + 1) * sizeof(double), s));
   const int gv = nparts;
   const int gs = grid_for(D, 256, p->ctx->num_sms * 8);
-  // reorthogonalisation dots: element chunks of ~1024 (>= 32 elements per lane per vector)
-  const int gmd = (int)std::max<int64_t>(1, std::min<int64_t>((D + 1023) / 1024, nparts));
+  // reorthogonalisation dots: element chunks of one tile (RD_TILE) per block where the
+  // partial store (nparts blocks) allows it
+  const int gmd = (int)std::max<int64_t>(1, std::min<int64_t>((D + RD_TILE - 1) / RD_TILE, nparts));
   auto qv = [&](int k) -> double* { return Q + (int64_t)(store ? k : (k % 3)) * D; };
   // q_0
   if (d_v0) {
