@@ -126,89 +126,103 @@ __global__ void k_lz_update(double* __restrict__ w, const double* __restrict__ q
 }
 
 // ---- full reorthogonalisation: classical Gram-Schmidt against Q[0..m) -----------------------
-// h = Q^T w. Block b owns the element chunk [b*ch, (b+1)*ch) (ch = ceil(n / gridDim)); each warp
-// forms whole dot products of that chunk with vectors j = warp, warp + nwarps, ... and walks the
-// chunk in tiles of RD_TILE elements: each lane issues its RD_EPL loads of q_j and of w (w hits
-// L1 after the first vector) before the FMAs, so a warp keeps 2*RD_EPL loads in flight (the
-// Krylov store streams from HBM; with few loads in flight the kernel waits on latency, not on
-// the FP64 pipe). Four FMA chains per lane, shuffle reduction, partial[j*gridDim + b]; the last
-// block to finish sums the partials of every j in block order. No block-wide barrier per vector.
-constexpr int RD_EPL = 16;
+// h = Q^T w, pass 1: block b owns the element chunk [b*ch, (b+1)*ch) (ch = ceil(n / gridDim)) and
+// writes partial[j*gridDim + b] for every vector j. FP64 is the narrow pipe on this part, so the
+// kernel keeps its FP64 work close to one FMA per element and vector:
+//  * one-tile chunks (ch <= RD_TILE, the usual case): w stays in registers; a warp takes four
+//    vectors at a time, issues each vector's RD_EPL loads before its FMAs (two chains per lane),
+//    and folds the four per-lane sums with one transposing butterfly (6 adds per lane for four
+//    dot products instead of 4 x 5);
+//  * longer chunks: one vector per warp, tiles of RD_TILE, q and w loads in flight together.
+// The partials are summed in block order by k_multidot_reduce (one block per vector).
+constexpr int RD_EPL = 20;  // even (two FMA chains); 640-element tiles, two CTAs per SM
 constexpr int RD_TILE = 32 * RD_EPL;
-__global__ void __launch_bounds__(LZ_NT) k_multidot(const double* __restrict__ Q, int64_t ldq, int m,
+__device__ __forceinline__ double rd_tile_dot(const double* __restrict__ q, const double (&wr)[RD_EPL], int64_t i0,
+                                              int64_t i1, int lane) {
+  double qv[RD_EPL];
+#pragma unroll
+  for (int e = 0; e < RD_EPL; ++e) {
+    const int64_t i = i0 + lane + 32 * e;
+    qv[e] = i < i1 ? __ldg(q + i) : 0.0;
+  }
+  double a0 = 0.0, a1 = 0.0;
+#pragma unroll
+  for (int e = 0; e < RD_EPL; e += 2) {
+    a0 = fma(qv[e], wr[e], a0);
+    a1 = fma(qv[e + 1], wr[e + 1], a1);
+  }
+  return a0 + a1;
+}
+__global__ void __launch_bounds__(LZ_NT, 2) k_multidot(const double* __restrict__ Q, int64_t ldq, int m,
                                                     const double* __restrict__ w, int64_t n, double* partial,
-                                                    double* h, LzState* st) {
+                                                    LzState* st) {
   if (lz_stopped(st)) return;
   const int64_t ch = (n + gridDim.x - 1) / gridDim.x;
   const int64_t i0 = (int64_t)blockIdx.x * ch;
   const int64_t i1 = min(n, i0 + ch);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if (i1 - i0 <= RD_TILE) {
-    // one tile per block: w stays in registers for every vector (one load per FMA)
     double wr[RD_EPL];
 #pragma unroll
     for (int e = 0; e < RD_EPL; ++e) {
       const int64_t i = i0 + lane + 32 * e;
       wr[e] = i < i1 ? __ldg(w + i) : 0.0;
     }
+    for (int j0 = 4 * warp; j0 < m; j0 += 4 * nw) {
+      double p[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v)  // j0 + v < m is uniform across the warp
+        p[v] = (j0 + v < m) ? rd_tile_dot(Q + (int64_t)(j0 + v) * ldq, wr, i0, i1, lane) : 0.0;
+      // butterfly over the four sums: after the xor-16 and xor-8 exchanges each lane holds one
+      // vector's partial (vector 2*bit4 + bit3 of the lane id), then three more halvings
+      const bool hi = lane & 16, b8 = lane & 8;
+      const double k0 = (hi ? p[2] : p[0]) + __shfl_xor_sync(0xffffffffu, hi ? p[0] : p[2], 16);
+      const double k1 = (hi ? p[3] : p[1]) + __shfl_xor_sync(0xffffffffu, hi ? p[1] : p[3], 16);
+      double t = (b8 ? k1 : k0) + __shfl_xor_sync(0xffffffffu, b8 ? k0 : k1, 8);
+      t += __shfl_xor_sync(0xffffffffu, t, 4);
+      t += __shfl_xor_sync(0xffffffffu, t, 2);
+      t += __shfl_xor_sync(0xffffffffu, t, 1);
+      const int v = (hi ? 2 : 0) + (b8 ? 1 : 0);
+      if ((lane & 7) == 0 && j0 + v < m) partial[(int64_t)(j0 + v) * gridDim.x + blockIdx.x] = t;
+    }
+  } else {
     for (int j = warp; j < m; j += nw) {
       const double* q = Q + (int64_t)j * ldq;
-      double qv[RD_EPL];
-#pragma unroll
-      for (int e = 0; e < RD_EPL; ++e) {
-        const int64_t i = i0 + lane + 32 * e;
-        qv[e] = i < i1 ? __ldg(q + i) : 0.0;
-      }
       double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      for (int64_t t0 = i0; t0 < i1; t0 += RD_TILE) {
+        double qv[RD_EPL], wv[RD_EPL];
 #pragma unroll
-      for (int e = 0; e < RD_EPL; e += 4) {
-        a0 = fma(qv[e], wr[e], a0);
-        a1 = fma(qv[e + 1], wr[e + 1], a1);
-        a2 = fma(qv[e + 2], wr[e + 2], a2);
-        a3 = fma(qv[e + 3], wr[e + 3], a3);
+        for (int e = 0; e < RD_EPL; ++e) {
+          const int64_t i = t0 + lane + 32 * e;
+          const bool ok = i < i1;
+          qv[e] = ok ? __ldg(q + i) : 0.0;
+          wv[e] = ok ? __ldg(w + i) : 0.0;
+        }
+#pragma unroll
+        for (int e = 0; e < RD_EPL; e += 4) {
+          a0 = fma(qv[e], wv[e], a0);
+          a1 = fma(qv[e + 1], wv[e + 1], a1);
+          a2 = fma(qv[e + 2], wv[e + 2], a2);
+          a3 = fma(qv[e + 3], wv[e + 3], a3);
+        }
       }
       double acc = (a0 + a1) + (a2 + a3);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
       if (lane == 0) partial[(int64_t)j * gridDim.x + blockIdx.x] = acc;
     }
-  } else {
-  for (int j = warp; j < m; j += nw) {
-    const double* q = Q + (int64_t)j * ldq;
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    for (int64_t t0 = i0; t0 < i1; t0 += RD_TILE) {
-      double qv[RD_EPL], wv[RD_EPL];
-#pragma unroll
-      for (int e = 0; e < RD_EPL; ++e) {
-        const int64_t i = t0 + lane + 32 * e;
-        const bool ok = i < i1;
-        qv[e] = ok ? __ldg(q + i) : 0.0;
-        wv[e] = ok ? __ldg(w + i) : 0.0;
-      }
-#pragma unroll
-      for (int e = 0; e < RD_EPL; e += 4) {
-        a0 = fma(qv[e], wv[e], a0);
-        a1 = fma(qv[e + 1], wv[e + 1], a1);
-        a2 = fma(qv[e + 2], wv[e + 2], a2);
-        a3 = fma(qv[e + 3], wv[e + 3], a3);
-      }
-    }
-    double acc = (a0 + a1) + (a2 + a3);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) partial[(int64_t)j * gridDim.x + blockIdx.x] = acc;
   }
-  }
-  if (last_block(&st->ticket[2])) {
-    for (int j = warp; j < m; j += nw) {
-      double acc = 0.0;
-      for (int b = lane; b < (int)gridDim.x; b += 32) acc += ((volatile double*)partial)[(int64_t)j * gridDim.x + b];
+}
+
+// h = Q^T w, pass 2: block j sums partial[j*nb + b] over b in a fixed order (deterministic)
+__global__ void k_multidot_reduce(const double* __restrict__ partial, int nb, double* h, const LzState* st) {
+  if (lz_stopped(st)) return;
+  const int j = blockIdx.x, lane = threadIdx.x;
+  double acc = 0.0;
+  for (int b = lane; b < nb; b += 32) acc += partial[(int64_t)j * nb + b];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (lane == 0) h[j] = acc;
-    }
-    if (threadIdx.x == 0) st->ticket[2] = 0;
-  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) h[j] = acc;
 }
 
 // w -= sum_j h[j] Q[j]; optionally accumulates ||w||^2 and finalises beta_{k+1}. Each thread owns
@@ -478,9 +492,10 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
     uint64_t nl = 3;
     if (prm->reorth) {
       for (int pass = 0; pass < 2; ++pass) {
-        k_multidot<<<gmd, LZ_NT, 0, s>>>(Q, D, k + 1, w, D, part, h, st);
+        k_multidot<<<gmd, LZ_NT, 0, s>>>(Q, D, k + 1, w, D, part, st);
+        k_multidot_reduce<<<k + 1, 32, 0, s>>>(part, gmd, h, st);
         k_multiaxpy<<<gv, LZ_NT, 0, s>>>(Q, D, k + 1, h, w, D, part, st, d_beta + k + 1, k, pass == 1, d_alpha + k);
-        nl += 2;
+        nl += 3;
       }
     }
     k_scale<<<gs, 256, 0, s>>>(w, qv(k + 1), D, d_beta + k + 1, stopf);
