@@ -471,7 +471,13 @@ BLayout blayout(const ed_plan_s* p, int B, int K, int c) {
   BLayout L;
   const int64_t D = p->dim;
   L.nvec = std::max(4, 2 * c + 6);
-  L.gx = (int)std::max<int64_t>(1, std::min<int64_t>((D + 4 * BT_NT - 1) / (4 * BT_NT), 64));
+  // CTAs per problem of the streaming kernels: no more than one resident wave over all B
+  // problems. Every CTA ends with one to five block sums in FP64 (the narrow pipe here), so at
+  // large B fewer, longer CTAs cut that overhead (forward 97 -> 90 ms at B = 64, D = 63,504).
+  // The parameter-term CTAs keep up to 64 per problem: with fewer the reverse sweep got slower.
+  const int64_t wave = (int64_t)p->ctx->num_sms * (2048 / BT_NT);  // 256-thread CTAs at full occupancy
+  L.gx = (int)std::max<int64_t>(
+      1, std::min<int64_t>({(D + 4 * BT_NT - 1) / (4 * BT_NT), (int64_t)64, (wave + B - 1) / B}));
   L.nsw = (int)std::max<int64_t>(1, std::min<int64_t>((D + 4 * SW_NT - 1) / (4 * SW_NT), 64));
   size_t o = 0;
   L.off_vec = o; o = bt_align(o + (size_t)L.nvec * B * D * sizeof(double));
