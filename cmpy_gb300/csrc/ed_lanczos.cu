@@ -43,11 +43,12 @@ __device__ __forceinline__ bool last_block(unsigned int* ticket) {
   return am_last;
 }
 
-// sum partials[0..n) with the whole block, in a fixed order
+// sum partials[0..n) with the whole block (NT threads), in a fixed order
+template <int NT = LZ_NT>
 __device__ double block_sum_array(const double* p, int n, double* smem) {
   double v = 0.0;
-  for (int i = threadIdx.x; i < n; i += LZ_NT) v += ((volatile const double*)p)[i];
-  return block_sum<LZ_NT>(v, smem);
+  for (int i = threadIdx.x; i < n; i += NT) v += ((volatile const double*)p)[i];
+  return block_sum<NT>(v, smem);
 }
 
 // ---- start vector ------------------------------------------------------------------------
@@ -226,25 +227,27 @@ __global__ void k_multidot_reduce(const double* __restrict__ partial, int nb, do
 }
 
 // w -= sum_j h[j] Q[j]; optionally accumulates ||w||^2 and finalises beta_{k+1}. Each thread owns
-// two elements per grid-stride step (i and i + LZ_NT, each coalesced across the warp), so one
+// two elements per grid-stride step (i and i + RA_NT, each coalesced across the warp), so one
 // shared-memory read of h_j serves two FMAs, and walks j in groups of RA_J: the 2*RA_J loads of a
-// group are issued before their FMAs (four chains per element). m <= RO_MAX (checked by the host).
+// group are issued before their FMAs (four chains per element). Small CTAs (2*RA_NT elements)
+// spread the last partial wave evenly over the SMs. m <= RO_MAX (checked by the host).
 constexpr int RO_MAX = 1024;
 constexpr int RA_J = 8;
-__global__ void __launch_bounds__(LZ_NT, 3) k_multiaxpy(const double* __restrict__ Q, int64_t ldq, int m,
+constexpr int RA_NT = 128;
+__global__ void __launch_bounds__(RA_NT, 6) k_multiaxpy(const double* __restrict__ Q, int64_t ldq, int m,
                                                      const double* __restrict__ h, double* __restrict__ w, int64_t n,
                                                      double* partial, LzState* st, double* beta_next, int k,
                                                      int final_norm, const double* alpha_k) {
   if (lz_stopped(st)) return;
-  __shared__ double sm[LZ_NT / 32];
+  __shared__ double sm[RA_NT / 32];
   __shared__ double hs[RO_MAX + RA_J];
-  for (int j = threadIdx.x; j < m + RA_J; j += LZ_NT) hs[j] = j < m ? h[j] : 0.0;
+  for (int j = threadIdx.x; j < m + RA_J; j += RA_NT) hs[j] = j < m ? h[j] : 0.0;
   __syncthreads();
   double v = 0.0;
   const int mf = m - m % RA_J;  // vectors in full groups
-  const int64_t step = (int64_t)gridDim.x * 2 * LZ_NT;
-  for (int64_t ia = blockIdx.x * (int64_t)(2 * LZ_NT) + threadIdx.x; ia < n; ia += step) {
-    const int64_t ib = ia + LZ_NT;
+  const int64_t step = (int64_t)gridDim.x * 2 * RA_NT;
+  for (int64_t ia = blockIdx.x * (int64_t)(2 * RA_NT) + threadIdx.x; ia < n; ia += step) {
+    const int64_t ib = ia + RA_NT;
     const bool hb = ib < n;
     const int64_t ibc = hb ? ib : ia;  // a valid address for the second element's loads
     double xa0 = w[ia], xa1 = 0.0, xa2 = 0.0, xa3 = 0.0;
@@ -282,10 +285,10 @@ __global__ void __launch_bounds__(LZ_NT, 3) k_multiaxpy(const double* __restrict
       v = fma(xb, xb, v);
     }
   }
-  v = block_sum<LZ_NT>(v, sm);
+  v = block_sum<RA_NT>(v, sm);
   if (threadIdx.x == 0) partial[blockIdx.x] = v;
   if (last_block(&st->ticket[3])) {
-    const double s = block_sum_array(partial, gridDim.x, sm);
+    const double s = block_sum_array<RA_NT>(partial, gridDim.x, sm);
     if (threadIdx.x == 0) {
       st->nrm2 = s;
       if (final_norm) {
@@ -448,6 +451,9 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
   // reorthogonalisation dots: element chunks of one tile (RD_TILE) per block where the
   // partial store (nparts blocks) allows it
   const int gmd = (int)std::max<int64_t>(1, std::min<int64_t>((D + RD_TILE - 1) / RD_TILE, nparts));
+  // reorthogonalisation axpy: one CTA per 2*RA_NT elements, at most 2*nparts CTAs (their norm
+  // partials fit the partial store, which holds nparts * (K + 2) values)
+  const int gax = (int)std::max<int64_t>(1, std::min<int64_t>((D + 2 * RA_NT - 1) / (2 * RA_NT), 2 * (int64_t)nparts));
   auto qv = [&](int k) -> double* { return Q + (int64_t)(store ? k : (k % 3)) * D; };
   // q_0
   if (d_v0) {
@@ -494,7 +500,7 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
       for (int pass = 0; pass < 2; ++pass) {
         k_multidot<<<gmd, LZ_NT, 0, s>>>(Q, D, k + 1, w, D, part, st);
         k_multidot_reduce<<<k + 1, 32, 0, s>>>(part, gmd, h, st);
-        k_multiaxpy<<<gv, LZ_NT, 0, s>>>(Q, D, k + 1, h, w, D, part, st, d_beta + k + 1, k, pass == 1, d_alpha + k);
+        k_multiaxpy<<<gax, RA_NT, 0, s>>>(Q, D, k + 1, h, w, D, part, st, d_beta + k + 1, k, pass == 1, d_alpha + k);
         nl += 3;
       }
     }
