@@ -98,3 +98,21 @@ def test_chain_lattice():
     assert ChainLattice(4, True).neighbors(0) == [1, 3]
     pairs, _ = ChainLattice(4, True).neighbor_pairs(True)
     assert pairs.tolist() == [[0, 1], [0, 3], [1, 2], [2, 3]]
+
+
+def test_apply_fermion_batch_checks_lengths_before_any_device_work():
+    """Mismatched plan / target / offset lists are rejected on the host."""
+    from cmpy_gb300 import engine as E
+
+    with pytest.raises(ValueError):
+        E.apply_fermion_batch([object(), object()], [object()], 0, 1, True, None, [0, 1])
+    with pytest.raises(ValueError):
+        E.apply_fermion_batch([object()], [object()], 0, 1, True, None, [0, 1])
+
+
+def test_model_plans_keeps_empty_slots():
+    """plans() maps a None sector to None (no plan is built for it)."""
+    from cmpy_gb300.models import ChainLattice, HubbardModel
+
+    m = HubbardModel(ChainLattice(4, False), inter=2.0, mu=1.0)
+    assert m.plans([None, None]) == [None, None]
