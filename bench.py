@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and adjoint measurements")
     ap.add_argument("--matvec-only", type=int, default=0,
                     help="time N fixed-point matvecs of the 14-site sector alone (kernel profiling)")
+    ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES), default=None,
+                    help="run one small single-kernel workload once (for ncu captures) and exit")
     return ap.parse_args()
 
 
@@ -76,6 +78,72 @@ def run_matvec_only(n: int):
     mean = sum(us) / n
     print(json.dumps({"kernel": "k_bfp_hub_matvec", "variant": os.environ.get("CMPY_ED_MATVEC", "auto"), "dim": plan.dim, "matvec_us_mean": round(mean, 2),
                       "matvec_us_min": round(min(us), 2), "gbs": round(16.0 * plan.dim / (mean * 1e-6) / 1e9, 1)}))
+
+
+def case_gf14(steps: int = 12) -> None:
+    """Particle-sector Lanczos of the 14-site Hubbard ring (U=4, mu=2, t=1), sector (8,7),
+    D = 10,306,296, from a seeded uniform start vector, 12 steps in block fixed point (three
+    rotating vectors, ~0.5 GB on the device): the update kernel and the integer matvec of the
+    benchmark step without its 23.6 GB Krylov store."""
+    import torch
+
+    from cmpy_gb300 import engine as E
+    from cmpy_gb300.models import ChainLattice, HubbardModel
+
+    m = HubbardModel(ChainLattice(14, True), inter=4.0, mu=2.0, hop=1.0)
+    p = m.plan(8, 7)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    s = torch.rand(p.dim, dtype=torch.float64, device="cuda", generator=g)
+    a, b, _ = E.lanczos_coeffs(p, s, max_steps=steps)
+    torch.cuda.synchronize()
+    print(f"gf14: {a.numel()} steps, alpha_0 = {float(a[0]):.12f}")
+
+
+def case_adjoint64(n: int = 64) -> None:
+    """The batched part of the `adjoint` extra: 64 SIAMs with 1 impurity + 9 bath sites,
+    sector (5,5), 1024 Matsubara frequencies at beta=100, seeded bath parameters (numpy
+    default_rng(5)); forward and backward once."""
+    import torch
+
+    from cmpy_gb300.adjoint import greens_function_ad_batch, siam_parameters
+
+    rng = np.random.default_rng(5)
+    z = 1j * (2 * np.arange(1024) + 1) * np.pi / 100.0
+    eb = torch.tensor(rng.uniform(-2, 2, (n, 9)), dtype=torch.float64, device="cuda", requires_grad=True)
+    v = torch.tensor(rng.uniform(0.1, 0.6, (n, 9)), dtype=torch.float64, device="cuda", requires_grad=True)
+    u = torch.tensor(4.0, dtype=torch.float64, device="cuda")
+    e_imp = torch.tensor(0.0, dtype=torch.float64, device="cuda")
+    rows = [siam_parameters(u, e_imp, eb[i], v[i]) for i in range(n)]
+    th = torch.stack([r[0] for r in rows])
+    n_sites, bonds, width = rows[0][1], rows[0][2], rows[0][3]
+    g = greens_function_ad_batch(th, n_sites, bonds, (5, 5), z, sign_width=width, gs_steps=250, gf_levels=150,
+                                 ckpt=16)
+    torch.sum(torch.abs(g) ** 2).backward()
+    torch.cuda.synchronize()
+    print(f"adjoint64: |grad| = {float(eb.grad.abs().sum() + v.grad.abs().sum()):.6f}")
+
+
+def case_sweep10() -> None:
+    """The `batched_sweep` workload (all 121 sectors of the 10-site Hubbard ring, U=6, mu=3,
+    t=1; 300 steps, tol 1e-12, tested every 10 steps) in one batched launch with a fixed
+    configuration (512 threads, 2 CTAs per SM, clusters of 4 CTAs), run twice (the second
+    launch is the one to capture)."""
+    import torch
+
+    from cmpy_gb300.batched import Batch
+    from cmpy_gb300.models import ChainLattice, HubbardModel
+
+    m = HubbardModel(ChainLattice(10, True), inter=6.0, mu=3.0, hop=1.0)
+    plans = [m.plan(nu, nd) for nu, nd in m.basis.iter_fillings()]
+    b = Batch(plans)
+    b.threads, b.ctas_per_sm, b.cluster_size = 512, 2, 4
+    for _ in range(2):
+        r = b.lanczos(max_steps=300, tol=1e-12, check_every=10)
+    torch.cuda.synchronize()
+    print(f"sweep10: {len(plans)} sectors, E0 = {float(r.energy.min()):.12f}")
+
+
+PROFILE_CASES = {"gf14": case_gf14, "adjoint64": case_adjoint64, "sweep10": case_sweep10}
 
 
 def peaks():
@@ -302,7 +370,9 @@ def run_ours(args, rank, world, dist):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "int64",
+        "arithmetic": ("int64 block fixed point (56-bit mantissas, one exponent per vector) for the Krylov vectors "
+                       "and H*v; FP64 for alpha, beta, the tridiagonal solve and the continued fraction"),
         "data": "synthetic (deterministic model, seeded uniform start vector)",
         "config": {
             "workload": "hubbard_ring14_half_filling_gs250_cf200",
@@ -384,9 +454,28 @@ def run_batched_sweep():
     }
 
 
-def run_disorder_batch(n_real: int = 512, n_freq: int = 1024):
+def _dense_lehmann(plan_gs, plan_t, psi, e0, z, create: bool):
+    """T=0 Lehmann sum of one neighbouring sector from its dense eigenpairs (device eigh):
+    the accuracy check of the continued fractions on the real axis."""
+    import torch
+
+    H = plan_t.dense()
+    w, V = torch.linalg.eigh(H)
+    phi = plan_gs.apply_fermion(plan_t, 0, 1, create, psi)
+    amp = (V.T @ phi) ** 2
+    zt = torch.as_tensor(z).cuda()
+    if create:
+        return (amp[None, :] / (zt[:, None] - (w[None, :] - e0))).sum(1)
+    return (amp[None, :] / (zt[:, None] + (w[None, :] - e0))).sum(1)
+
+
+def run_disorder_batch(n_real: int = 512, n_freq: int = 1024, n_dense: int = 8):
     """Batched disorder: realisations of the 8-site Anderson-Hubbard chain (eps ~ U[-1,1],
-    U=4, t=1, n_up, n_dn ~ U{2..5}); ground state + G(w) at n_freq real frequencies each."""
+    U=4, t=1, mu=2, n_up, n_dn ~ U{2..5}, numpy default_rng(2024)); ground state + G(w) at
+    n_freq real frequencies in [-8, 8] (eta = 0.05) and 256 Matsubara points (beta = 10) each.
+    1000 Lanczos levels (no reorthogonalisation) converge the continued fractions on the real
+    axis; the accuracy is checked against dense-eigh Lehmann sums on `n_dense` realisations
+    (the largest sectors first) and against the per-realisation runs."""
     import torch
 
     from cmpy_gb300.batched import greens_functions_batched
@@ -397,14 +486,9 @@ def run_disorder_batch(n_real: int = 512, n_freq: int = 1024):
     lat = ChainLattice(8, False)
     models = [HubbardModel(lat, inter=4.0, eps=rng.uniform(-1, 1, 8), mu=2.0, hop=1.0) for _ in range(n_real)]
     sectors = [(int(a), int(b)) for a, b in rng.integers(2, 6, size=(n_real, 2))]
-    # n_freq real frequencies (eta = 0.05) plus 256 Matsubara points at beta = 10: there the
-    # 150-level continued fractions are converged, so batched and per-realisation results must
-    # agree to rounding; on the real axis both are 150-level continued fractions whose
-    # truncation error at eta = 0.05 (up to ~0.3 against the exact Lehmann sum for the largest
-    # sectors) dominates their difference
     n_mats = 256
     z = np.concatenate([np.linspace(-8, 8, n_freq) + 0.05j, 1j * (2 * np.arange(n_mats) + 1) * np.pi / 10.0])
-    levels = 150
+    levels = 1000
     for m_, s_ in zip(models, sectors):  # plans (setup, untimed)
         for d in (-1, 0, 1):
             m_.plan(s_[0] + d, s_[1])
@@ -417,14 +501,23 @@ def run_disorder_batch(n_real: int = 512, n_freq: int = 1024):
         out = []
         for m_, (a, b) in zip(models[:n_plain], sectors[:n_plain]):
             e0, psi = groundstate_sector(m_, a, b, max_steps=300, tol=1e-12)
-            out.append((e0, gf_continued_fraction(m_, z, a, b, e0, psi, n_lev=levels)))
+            out.append((e0, psi, gf_continued_fraction(m_, z, a, b, e0, psi, n_lev=levels)))
         return out
 
     plain()
     pl, t_plain = _timed(plain)
-    gdiff = max(float(np.max(np.abs(gb[i].cpu().numpy()[:n_freq] - pl[i][1][:n_freq]))) for i in range(n_plain))
-    gdiff_m = max(float(np.max(np.abs(gb[i].cpu().numpy()[n_freq:] - pl[i][1][n_freq:]))) for i in range(n_plain))
+    gdiff = max(float(np.max(np.abs(gb[i].cpu().numpy()[:n_freq] - pl[i][2][:n_freq]))) for i in range(n_plain))
+    gdiff_m = max(float(np.max(np.abs(gb[i].cpu().numpy()[n_freq:] - pl[i][2][n_freq:]))) for i in range(n_plain))
     ediff = max(abs(float(eb[i]) - pl[i][0]) / abs(pl[i][0]) for i in range(n_plain))
+    # dense check: the largest sectors among the plain sample
+    order = sorted(range(n_plain), key=lambda i: -models[i].plan(*sectors[i]).dim)[:n_dense]
+    derr = 0.0
+    for i in order:
+        m_, (a, b) = models[i], sectors[i]
+        e0, psi = pl[i][0], pl[i][1]
+        g_d = _dense_lehmann(m_.plan(a, b), m_.plan(a + 1, b), psi, e0, z, True)
+        g_d = g_d + _dense_lehmann(m_.plan(a, b), m_.plan(a - 1, b), psi, e0, z, False)
+        derr = max(derr, float(torch.max(torch.abs(gb[i] - g_d))))
     return {
         "workload": f"anderson_hubbard_chain8_{n_real}_realisations_gs_gf{n_freq}",
         "batched_ms": round(t_batch, 3),
@@ -434,6 +527,9 @@ def run_disorder_batch(n_real: int = 512, n_freq: int = 1024):
         "max_rel_energy_diff": ediff,
         "max_abs_gf_diff_matsubara": gdiff_m,
         "max_abs_gf_diff_real_axis": gdiff,
+        "max_abs_gf_err_vs_dense_eigh": derr,
+        "dense_checked": [list(sectors[i]) for i in order],
+        "eta": 0.05,
         "n_matsubara": n_mats,
         "gf_levels": levels,
     }
@@ -668,6 +764,9 @@ def main():
     dist = None
     if args.matvec_only:
         run_matvec_only(args.matvec_only)
+        return
+    if args.profile_case:
+        PROFILE_CASES[args.profile_case]()
         return
     if args.impl == "reference":
         out = run_reference(args, rank, world)

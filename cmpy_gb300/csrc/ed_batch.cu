@@ -796,7 +796,7 @@ ED_API ed_status ed_batch_destroy(ed_batch b) {
 ED_API ed_status ed_batch_workspace(ed_batch b, int max_steps, int threads, int ctas_per_sm, int cluster_size,
                                     size_t* bytes) {
   if (!b || !bytes) return fail(ED_ERR_INVALID_ARG, "null argument");
-  if (max_steps < 1 || max_steps > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  if (max_steps < 1 || max_steps > 4096) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 4096]");
   int t = threads, ps = ctas_per_sm, cs = cluster_size;
   if (t <= 0 || ps <= 0) default_config(b, &t, &ps, &cs);
   if (cs <= 0) cs = 1;
@@ -811,7 +811,7 @@ ED_API ed_status ed_batch_lanczos(ed_batch b, int max_steps, double tol, int che
                                   int32_t* d_steps, double* d_vecs, const int64_t* d_vec_offsets, int threads,
                                   int ctas_per_sm, int cluster_size, ed_stream_t stream) {
   if (!b) return fail(ED_ERR_INVALID_ARG, "null batch");
-  if (max_steps < 1 || max_steps > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  if (max_steps < 1 || max_steps > 4096) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 4096]");
   if (!d_alpha || !d_beta || !d_energy || !d_residual || !d_steps)
     return fail(ED_ERR_INVALID_ARG, "null output array");
   if (want_vector && (!d_vecs || !d_vec_offsets)) return fail(ED_ERR_INVALID_ARG, "want_vector needs vectors");

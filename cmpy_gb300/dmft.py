@@ -2,12 +2,13 @@
 
 Two parts:
 
-* the reference's two-site DMFT at half filling (cmpy/dmft/twosite.py:103-172) with its
-  helpers (self energy, Bethe-lattice Green's function, quasiparticle weight, mixing,
-  iteration statistics; cmpy/dmft/utils.py:66-260) and the analytic two-site solution of
-  E. Lange (twosite.py:25-84). The impurity Green's function comes from the engine
-  (`SingleImpurityAndersonModel.impurity_gf`, thermal Lehmann sum on the device) or, at
-  T = 0, from the ground state and the zero-temperature Lehmann sum;
+* two-site DMFT at half filling (the entry point of cmpy/dmft/twosite.py:103-172, written
+  here from the physics: V^2 = Z t^2 on the Bethe lattice) with the public helpers of
+  cmpy/dmft/utils.py (self energy, Bethe-lattice Green's function, quasiparticle weight,
+  mixing, iteration record) and E. Lange's closed-form two-site solution. The impurity
+  Green's function comes from the engine (`SingleImpurityAndersonModel.impurity_gf`, thermal
+  Lehmann sum on the device) or, at T = 0, from the ground state and the zero-temperature
+  Lehmann sum;
 * a multi-bath DMFT loop on the Matsubara axis for the Bethe lattice with a bath fit that
   uses the adjoint Green's function (`cmpy_gb300.adjoint`): the bath energies and
   hybridisations are fitted so that the impurity Green's function of the SIAM matches a
@@ -48,125 +49,120 @@ __all__ = [
 
 
 # ------------------------------------------------------------------------------------------
-# helpers (cmpy/dmft/utils.py)
+# loop bookkeeping and the Green's-function algebra of the DMFT cycle
+# (public names as cmpy/dmft/utils.py:66-275)
 # ------------------------------------------------------------------------------------------
 
 
 class IterationStats(Sequence):
-    """Errors per iteration and the convergence status (cmpy/dmft/utils.py:66-160)."""
+    """Record of a self-consistency loop: one row of monitored quantities (``labels``) per
+    iteration, and the outcome once the loop has ended (``success``, ``status``)."""
 
     def __init__(self, *labels):
-        super().__init__()
-        self._errors = []
-        self.labels = labels
+        self.labels = tuple(labels)
+        self._rows: list = []
         self.success = False
         self.status = ""
 
+    # the rows
+    def append(self, *values):
+        self._rows.append([float(np.real(v)) for v in values])
+
+    def __len__(self):
+        return len(self._rows)
+
+    def __getitem__(self, i):
+        return self._rows[i]
+
     @property
     def iteration(self):
-        return len(self._errors)
+        return len(self._rows)
 
     @property
     def errors(self):
-        return self._errors[-1]
+        """The monitored quantities of the latest iteration."""
+        return self._rows[-1]
 
     @property
     def history(self):
-        return np.asarray(self._errors).T
+        """Array [len(labels), iterations]."""
+        return np.array(self._rows, dtype=np.float64).T
+
+    # the outcome
+    def set_status(self, success, status=""):
+        self.success, self.status = bool(success), str(status)
+
+    def set_maxiter_status(self, maxiter):
+        self.set_status(False, f"stopped after {maxiter} iterations")
+
+    def set_parameter_converged(self, name, value, dec=4):
+        self.set_status(True, f"{name} settled at {value:.{dec}f}")
 
     @property
     def message(self):
-        msg = "Self-consistency reached" if self.success else "Self-consistency not reached"
-        return msg + ": " + self.status
-
-    def append(self, *items):
-        self._errors.append(list(items))
-
-    def set_status(self, success, status=""):
-        self.success = success
-        self.status = status
-
-    def set_maxiter_status(self, maxiter):
-        self.success = False
-        self.status = f"Maximum iteration of {maxiter} reached without converging!"
-
-    def set_parameter_converged(self, name, value, dec=4):
-        self.success = True
-        self.status = f"{name} converged to {value:.{dec}f}"
+        return ("converged" if self.success else "not converged") + (f" ({self.status})" if self.status else "")
 
     def __bool__(self):
         return self.success
 
-    def __len__(self):
-        return len(self._errors)
-
-    def __getitem__(self, i):
-        return self._errors[i]
-
     def __str__(self):
-        return f"{self.message} (iterations: {self.iteration})"
+        return f"{self.message} after {self.iteration} iterations"
 
 
 def mix_values(old, new, mixing=1.0):
-    """new * mixing + old * (1 - mixing); mixing = 1 returns `new` (cmpy/dmft/utils.py:163-185)."""
-    if mixing == 1:
-        return new
-    assert 0 < mixing < 1
-    return new * mixing + old * (1.0 - mixing)
+    """Linear mixing old + mixing * (new - old); mixing must lie in (0, 1]."""
+    if not 0 < mixing <= 1:
+        raise ValueError("mixing must lie in (0, 1]")
+    return new if mixing == 1 else old + mixing * (new - old)
 
 
 def self_energy(gf_imp0, gf_imp):
-    """Sigma(z) = G0(z)^-1 - G(z)^-1 (cmpy/dmft/utils.py:188-211)."""
-    return 1 / gf_imp0 - 1 / gf_imp
+    """Dyson equation: Sigma(z) = G0(z)^-1 - G(z)^-1."""
+    return 1.0 / gf_imp0 - 1.0 / gf_imp
 
 
 def bethe_gf_omega(z, t: float):
-    """Local Green's function of the Bethe lattice (infinite coordination, hopping t)
-    (cmpy/dmft/utils.py:214-230)."""
-    z_rel = z / (2 * t)
-    return z_rel * (1 - np.sqrt(1 - 1 / (z_rel * z_rel))) / t
+    """Local Green's function of the Bethe lattice with hopping t (semicircular density of
+    states of half-width 2t): G(z) = 2 / (z (1 + sqrt(1 - 4 t^2 / z^2))), the form that is
+    stable for large |z| and has Im G < 0 for Im z > 0."""
+    z = np.asarray(z, dtype=np.complex128)
+    return 2.0 / (z * (1.0 + np.sqrt(1.0 - 4.0 * t * t / (z * z))))
 
 
 def quasiparticle_weight(omegas, sigma, thresh: float = 1e-5):
-    """z_qp = [1 - dRe Sigma/domega (0)]^-1 from a linear fit over the frequencies within one
-    grid step of 0; set to 0 below `thresh` (cmpy/dmft/utils.py:233-275)."""
-    omegas = np.asarray(omegas)
-    sigma = np.asarray(sigma)
-    dw = omegas[1] - omegas[0]
-    win = (-dw <= omegas) * (omegas <= +dw)
-    try:
-        dsigma = np.polyfit(omegas[win], sigma.real[win], 1)[0]
-    except np.linalg.LinAlgError:
-        omega_win = omegas[win]
-        sigma_win = sigma[win]
-        dsigma = (sigma_win[-1] - sigma_win[0]) / (omega_win[-1] - omega_win[0])
-    z_qp = 1 / (1 - dsigma)
-    if z_qp < thresh:
-        z_qp = 0
-    return z_qp
+    """Z = 1 / (1 - d Re Sigma / d omega) at omega = 0, the slope taken as the central
+    difference of Re Sigma interpolated one grid step on either side of 0; Z below `thresh`
+    counts as 0 (an insulator)."""
+    w = np.asarray(omegas, dtype=np.float64)
+    s = np.asarray(sigma).real
+    h = abs(w[1] - w[0])
+    slope = (np.interp(h, w, s) - np.interp(-h, w, s)) / (2.0 * h)
+    z_qp = 1.0 / (1.0 - slope)
+    return 0 if z_qp < thresh else z_qp
 
 
 # ------------------------------------------------------------------------------------------
-# two-site DMFT (cmpy/dmft/twosite.py)
+# two-site DMFT (the scheme of M. Potthoff; reference driver cmpy/dmft/twosite.py:103-172)
 # ------------------------------------------------------------------------------------------
 
 
 def impurity_params_ref(u: float, v: float):
-    """Residues and poles of the two-site SIAM Green's function at half filling and T = 0
-    (E. Lange; cmpy/dmft/twosite.py:25-60): (alpha_1, alpha_2, omega_1, omega_2)."""
-    sqrt16 = np.sqrt(u**2 + 16 * v**2)
-    sqrt64 = np.sqrt(u**2 + 64 * v**2)
-    a1 = 0.25 * (1 - (u**2 - 32 * v**2) / np.sqrt((u**2 + 64 * v**2) * (u**2 + 16 * v**2)))
-    a2 = 0.5 - a1
-    e1 = 0.25 * (sqrt64 - sqrt16)
-    e2 = 0.25 * (sqrt64 + sqrt16)
-    return float(a1), float(a2), float(e1), float(e2)
+    """Closed-form Green's function of the half-filled two-site Anderson impurity at T = 0
+    (E. Lange): four poles at +-omega_1, +-omega_2 with weights alpha_1, alpha_2,
+    omega_{1,2} = (sqrt(U^2 + 64 V^2) -+ sqrt(U^2 + 16 V^2)) / 4,
+    alpha_1 = (1 - (U^2 - 32 V^2) / sqrt((U^2 + 64 V^2)(U^2 + 16 V^2))) / 4, alpha_2 = 1/2 - alpha_1.
+    Returns (alpha_1, alpha_2, omega_1, omega_2)."""
+    r64, r16 = np.sqrt(u * u + 64.0 * v * v), np.sqrt(u * u + 16.0 * v * v)
+    alpha1 = 0.25 - 0.25 * (u * u - 32.0 * v * v) / (r64 * r16)
+    return float(alpha1), float(0.5 - alpha1), float(0.25 * (r64 - r16)), float(0.25 * (r64 + r16))
 
 
 def impurity_gf_ref(z, u: float, v: float):
-    """Analytic two-site impurity Green's function (cmpy/dmft/twosite.py:63-84)."""
-    a1, a2, e1, e2 = impurity_params_ref(u, v)
-    return (a1 / (z - e1) + a1 / (z + e1)) + (a2 / (z - e2) + a2 / (z + e2))
+    """Lange's two-site impurity Green's function, each +-omega pole pair combined:
+    sum_k alpha_k 2 z / (z^2 - omega_k^2)."""
+    a1, a2, w1, w2 = impurity_params_ref(u, v)
+    z = np.asarray(z, dtype=np.complex128)
+    return 2.0 * z * (a1 / (z * z - w1 * w1) + a2 / (z * z - w2 * w2))
 
 
 def impurity_gf0(z, siam):
@@ -183,69 +179,55 @@ def _impurity_gf_t0(z, siam: SingleImpurityAndersonModel):
 
 
 def compute_impurity_gf(z, siam, ref=False):
-    """Impurity Green's function: Lange's analytic two-site result (ref=True) or the engine
-    (thermal Lehmann sum on the device; ground state + T = 0 Lehmann sum when temp = 0)."""
+    """Impurity Green's function: Lange's closed form (ref=True) or the engine (thermal
+    Lehmann sum on the device; ground state + T = 0 Lehmann sum when temp = 0)."""
     if ref:
         return impurity_gf_ref(z, float(np.atleast_1d(siam.u)[0]), float(siam.v[0]))
-    if siam.temp == 0:
-        return _impurity_gf_t0(z, siam)
-    return siam.impurity_gf(z)
+    return _impurity_gf_t0(z, siam) if siam.temp == 0 else siam.impurity_gf(z)
 
 
 def compute_self_energy(z, siam, ref=False):
-    gf_imp0 = impurity_gf0(z, siam)
-    gf_imp = compute_impurity_gf(z, siam, ref=ref)
-    return self_energy(gf_imp0, gf_imp)
+    return self_energy(impurity_gf0(z, siam), compute_impurity_gf(z, siam, ref=ref))
 
 
 def twosite_dmft_half_filling(z, u, t=1.0, beta=np.inf, mixing=1.0, vtol=1e-6, max_iter=1000, vthresh=1e-10,
                               verbose=True, ref=True):
-    """Two-site DMFT of the half-filled Hubbard model on the Bethe lattice (M. Potthoff's
-    scheme, cmpy/dmft/twosite.py:103-172): the bath hybridisation is updated to
-    v = sqrt(z_qp * m2) with m2 = t^2 until it changes by less than vtol. Returns the SIAM
-    (its ``stats`` attribute holds the iteration history)."""
-    siam = SingleImpurityAndersonModel(u, v=[t], mu=u / 2, temp=0.0 if not np.isfinite(beta) else 1 / beta)
-    v = siam.v[0] + 0.1  # the first update must differ from the initial value
-    m2 = t**2
-    it = 0
-    stats = IterationStats("Δv")
-    while True:
+    """Two-site DMFT of the half-filled Hubbard model on the Bethe lattice. The bath of the
+    one-bath-site impurity is fixed by matching the low-frequency weight of the lattice: the
+    hybridisation obeys V^2 = Z t^2 with Z the quasiparticle weight of the impurity self
+    energy. Starting from the free value V = t, the map V -> sqrt(Z(V)) t is iterated (with
+    linear mixing) until V moves by less than `vtol`, Z vanishes (Mott insulator) or
+    `max_iter` is reached. Returns the SIAM at the fixed point; its ``stats`` attribute holds
+    the history of |dV|."""
+    temp = 1.0 / beta if np.isfinite(beta) else 0.0
+    siam = SingleImpurityAndersonModel(u, v=[t], mu=u / 2, temp=temp)
+    stats = IterationStats("dv")
+    omegas = np.asarray(z).real
+    v = float(t)
+    for _ in range(max_iter + 1):
         siam.update_hybridization(v)
-        gf_imp0 = impurity_gf0(z, siam)
-        gf_imp = compute_impurity_gf(z, siam, ref=ref)
-        sigma = self_energy(gf_imp0, gf_imp)
-        qp_weight = quasiparticle_weight(z.real, sigma, thresh=vthresh)
-        v_new = mix_values(v, np.sqrt(qp_weight * m2), mixing=mixing)
-        delta_v = np.linalg.norm(v - v_new)
-        stats.append(delta_v)
-        v = v_new
-        if v == 0:
-            stats.set_parameter_converged("Hybridization", v)
+        z_qp = quasiparticle_weight(omegas, compute_self_energy(z, siam, ref=ref), thresh=vthresh)
+        v_next = float(mix_values(v, t * np.sqrt(z_qp), mixing=mixing))
+        stats.append(abs(v_next - v))
+        v = v_next
+        if z_qp == 0 or v == 0:
+            stats.set_parameter_converged("quasiparticle weight", 0.0)
             break
-        if delta_v < vtol:
-            stats.set_parameter_converged("Hybridization", v)
+        if stats.errors[0] < vtol:
+            stats.set_parameter_converged("hybridisation", v)
             break
-        elif qp_weight == 0:
-            stats.set_parameter_converged("Quasiparticle weight", qp_weight)
-            break
-        elif it >= max_iter:
-            stats.set_maxiter_status(max_iter)
-            break
-        it += 1
+    else:
+        stats.set_maxiter_status(max_iter)
     siam.update_hybridization(v)
     object.__setattr__(siam, "stats", stats)
     if verbose:
-        print("-" * 50)
-        print(f"U:          {u:.2f}")
-        print(stats)
+        print(f"two-site DMFT, U = {u:g}: V = {v:.8f}, {stats}")
     return siam
 
 
 def compute_lattice_greens_function(z, siam, t, ref=False):
-    """G_latt(z) = G_Bethe(z + mu - Sigma(z)) (cmpy/dmft/twosite.py:175-178)."""
-    mu = siam.mu
-    sigma = compute_self_energy(z, siam, ref)
-    return bethe_gf_omega(z + mu - sigma, t)
+    """Local lattice Green's function G_Bethe(z + mu - Sigma(z))."""
+    return bethe_gf_omega(z + siam.mu - compute_self_energy(z, siam, ref), t)
 
 
 # ------------------------------------------------------------------------------------------

@@ -46,83 +46,97 @@ __all__ = [
 
 
 class ModelParameters(MutableMapping):
-    """Parameters accessible as attributes or dict items (cmpy/models/abc.py:21-133)."""
+    """A model's named parameters, reachable both as attributes (``model.u``) and as mapping
+    items (``model["u"]``). The parameter names are the keyword arguments the constructor
+    received plus later ``set_param`` calls; every other attribute is an ordinary instance
+    attribute. Public surface as cmpy/models/abc.py:21-133.
+    """
 
     def __init__(self, **params):
-        MutableMapping.__init__(self)
-        self.__params__ = OrderedDict(params)
+        object.__setattr__(self, "_values", dict(params))
+
+    # ---- mapping over the parameters only ----------------------------------------------------
+    def __getitem__(self, name: str) -> Any:
+        return self._values[name]
+
+    def __setitem__(self, name: str, value: Any) -> None:
+        self._values[name] = value
+
+    def __delitem__(self, name: str) -> None:
+        self._values.pop(name)
+
+    def __iter__(self) -> Iterator[str]:
+        return iter(tuple(self._values))
+
+    def __len__(self) -> int:
+        return len(self._values)
+
+    # ---- attribute access: ordinary lookup first, then the parameters --------------------------
+    def __getattr__(self, name: str) -> Any:
+        values = self.__dict__.get("_values", {})
+        if name in values:
+            return values[name]
+        raise AttributeError(f"{type(self).__name__} has neither an attribute nor a parameter {name!r}")
+
+    def __setattr__(self, name: str, value: Any) -> None:
+        if name in self.__dict__.get("_values", {}):
+            self._values[name] = value
+        else:
+            object.__setattr__(self, name, value)
 
     @property
     def params(self) -> Dict[str, Any]:
-        return self.__params__
+        return self._values
 
     def set_param(self, key: str, value: Any) -> None:
-        self.__params__[key] = value
+        """Add (or overwrite) a parameter; it becomes an attribute of the model."""
+        self._values[key] = value
 
     def delete_param(self, key: str) -> None:
-        del self.__params__[key]
+        self._values.pop(key)
 
     def rename_param(self, key: str, new_key: str) -> None:
-        self.__params__[new_key] = self.__params__.pop(key)
+        """Rename a parameter in place (its position in the parameter order is kept)."""
+        self._values = {(new_key if k == key else k): v for k, v in self._values.items()}
 
-    def __len__(self) -> int:
-        return len(self.__params__)
-
-    def __getitem__(self, key: str) -> Any:
-        return self.__params__[key]
-
-    def __setitem__(self, key: str, value: Any) -> None:
-        self.__params__[key] = value
-
-    def __delitem__(self, key: str) -> None:
-        del self.__params__[key]
-
-    def __iter__(self) -> Iterator[str]:
-        return iter(self.__params__)
-
-    def __getattr__(self, key: str) -> Any:
-        key = str(key)
-        if not key.startswith("__") and key in self.__params__.keys():
-            return self.__params__[key]
-        return super().__getattribute__(key)
-
-    def __setattr__(self, key: str, value: Any) -> None:
-        key = str(key)
-        if not key.startswith("__") and key in self.__params__.keys():
-            self.__params__[key] = value
-        else:
-            super().__setattr__(key, value)
+    @staticmethod
+    def _fmt(value, decimals=None) -> str:
+        if decimals is not None and isinstance(value, (float, np.floating)):
+            return f"{float(value):.{decimals}f}"
+        return str(value)
 
     def key(self, decimals=None, delim="; "):
-        out = []
-        for k, v in self.__params__.items():
-            if decimals is not None and isinstance(v, (int, float)):
-                v = f"{v:.{decimals}f}"
-            out.append(f"{k}={v}")
-        return delim.join(out)
+        """One-line identifier of the parameter set, e.g. for cache keys or file names."""
+        return delim.join(f"{k}={self._fmt(v, decimals)}" for k, v in self._values.items())
 
     def json(self):
-        return json.dumps(self.__params__)
+        def plain(v):
+            if isinstance(v, np.ndarray):
+                return v.tolist()
+            if isinstance(v, np.generic):
+                return v.item()
+            return v
+
+        return json.dumps({k: plain(v) for k, v in self._values.items()})
 
     def pformat(self):
-        return ", ".join(f"{k}={v}" for k, v in self.__params__.items())
+        return ", ".join(f"{k}={self._fmt(v)}" for k, v in self._values.items())
 
     def __repr__(self) -> str:
-        return f"{self.__class__.__name__}({str(self.__params__)})"
+        return f"{type(self).__name__}({self.pformat()})"
 
     def __str__(self) -> str:
         return self.pformat()
 
 
 class AbstractModel(ModelParameters, ABC):
-    def __init__(self, **params):
-        ModelParameters.__init__(self, **params)
+    """Base of every model: a parameter set plus a Hamiltonian."""
 
     def __str__(self) -> str:
-        return f"{self.__class__.__name__}({ModelParameters.__str__(self)})"
+        return f"{type(self).__name__}({self.pformat()})"
 
     def hamiltonian(self, *args, **kwargs):
-        pass
+        raise NotImplementedError
 
 
 class _PlanCache:
@@ -155,7 +169,7 @@ class AbstractManyBodyModel(AbstractModel):
     """Fermionic many-body model on a Fock basis (cmpy/models/abc.py:206-260)."""
 
     def __init__(self, num_sites: Optional[int] = 0, **params):
-        super(AbstractModel, self).__init__(**params)
+        ModelParameters.__init__(self, **params)
         self.basis: Basis = Basis()
         self.init_basis(num_sites)
         object.__setattr__(self, "_plans", _PlanCache())
@@ -407,7 +421,7 @@ class AbstractSpinModel(AbstractModel):
     """Spin model on Sz sectors (cmpy/models/abc.py:160-203)."""
 
     def __init__(self, num_sites: Optional[int] = 0, **params):
-        super(AbstractModel, self).__init__(**params)
+        ModelParameters.__init__(self, **params)
         self.basis: SpinBasis = SpinBasis()
         self.init_basis(num_sites)
         object.__setattr__(self, "_plans", _PlanCache())

@@ -442,13 +442,17 @@ ED_API ed_status ed_matvec_fixed(ed_plan plan, const int64_t* d_xm, int32_t ex, 
                                  int32_t* h_ew, int* h_m_in, ed_stream_t stream);
 
 /* Allocation-free ed_tridiag_lowest (no counterpart in the reference). For callers that
- * cannot allocate device memory where they need the result — e.g. while one of their streams
- * is being captured into a CUDA graph, or when their device memory belongs to their own
- * allocator. The inverse-iteration scratch is a static array of the library's device image
- * holding 5 * 4096 doubles (160 KB on every GPU that loads the library), so m <= 4096 (larger
- * m returns ED_ERR_TOO_LARGE). The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) and must come before any stream capture on that device. All calls
- * share the array: calls that overlap on the GPU race on it. Allocates nothing. */
+ * cannot allocate device memory where they need the result: hosts whose device memory
+ * belongs to their own allocator (a framework's caching allocator or a fixed pool), plugin
+ * hosts that forbid libraries from allocating, and latency-critical loops where an
+ * allocation's bookkeeping or implicit synchronisation is not acceptable. The
+ * inverse-iteration scratch is a static array of the library's device image holding
+ * 5 * 4096 doubles (160 KB on every GPU that loads the library, until the process exits), so
+ * m <= 4096; larger m returns ED_ERR_INVALID_ARG, like ed_tridiag_lowest. The first call on a
+ * device (and the first after its context was replaced, e.g. by cudaDeviceReset) looks up the
+ * array's device address (cudaGetSymbolAddress); that call should come before any stream
+ * capture on the device. All calls share the array: calls that overlap on the GPU race on it.
+ * Calls no cudaMalloc / cudaFree and no allocating library routine. */
 ED_API ed_status ed_tridiag_lowest_noalloc(const double* d_alpha, const double* d_beta, int m,
                                            double* d_value, double* d_vec, ed_stream_t stream);
 

@@ -141,8 +141,9 @@ def test_heisenberg_coo_and_dense(cuda, golden, tag, n, periodic, j, jz, s):
     np.testing.assert_allclose(y, g[f"{tag}_y"], rtol=1e-14, atol=1e-14)
 
 
-def test_coo_14_site_counts(cuda):
-    """At 14 sites the whole-model generator matches the oracle's closed-form counts."""
+def test_coo_ring12_triplet_count(cuda):
+    """12-site ring (6,6): the whole-model generator emits the reference's triplet count
+    (13,737,108, counted by running the reference) and indexes inside the sector."""
     from cmpy_gb300.models import ChainLattice, HubbardModel
 
     m = HubbardModel(ChainLattice(12, True), inter=4.0, mu=2.0, hop=1.0)

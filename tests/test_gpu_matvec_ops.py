@@ -53,21 +53,55 @@ def test_matvec_vs_reference(cuda, golden, name):
         assert isinstance(yt, torch.Tensor) and yt.is_cuda
 
 
+def _ring14_slice(up_rows: int):
+    """Oracle CSR of the reference triplets whose origin lies in the first `up_rows` up-rows
+    of the 14-site ring (7,7) (U=4, mu=2, t=1)."""
+    import scipy.sparse as sp
+
+    up = O.sector_states(14, 7)
+    ring = [(i, (i + 1) % 14) if i < (i + 1) % 14 else ((i + 1) % 14, i) for i in range(14)]
+    eps, uu, bonds, width = O.hubbard_descriptor(14, ring, inter=4.0, hop=1.0, mu=2.0)
+    r, c, v = O.coo_fermion_rows(up, up, eps, uu, bonds, width, up_rows)
+    nd = len(up)
+    return sp.csr_matrix((v, (r, c)), shape=(up_rows * nd, len(up) * nd))
+
+
 def test_matvec_14site_properties(cuda):
-    """Full-size 14-site (7,7) sector: symmetry <x,Hy> = <Hx,y>, linearity, and agreement with
-    the device CSR of the reference triplets on a slice."""
+    """Full-size 14-site (7,7) sector: agreement with the oracle's CSR of the reference
+    triplets on the first 96 of 3432 up-rows (FP64 matvec to 1e-13; the fixed-point matvec
+    bit-exact on an integer vector, where every partial sum is an exact FP64 integer), plus
+    symmetry <x,Hy> = <Hx,y> and linearity on the whole sector."""
+    from cmpy_gb300 import engine as E
     from cmpy_gb300.models import ChainLattice, HubbardModel
 
     m = HubbardModel(ChainLattice(14, True), inter=4.0, mu=2.0, hop=1.0)
     p = m.plan(7, 7)
     assert p.dim == 3432 * 3432
+    rows = 96
+    csr = _ring14_slice(rows)
+    n = csr.shape[0]
+    rng = np.random.default_rng(14)
+    xh = rng.standard_normal(p.dim)
+    ref = csr @ xh
+    y = p.matvec(torch.as_tensor(xh).cuda())[:n].cpu().numpy()
+    np.testing.assert_allclose(y, ref, rtol=1e-13, atol=1e-13 * np.abs(ref).max())
+    xi = rng.integers(-(1 << 20), 1 << 20, size=p.dim).astype(np.int64)
+    wm, ew = p.matvec_fixed(torch.as_tensor(xi).cuda(), 0)
+    assert ew == 0
+    ref_i = csr @ xi.astype(np.float64)
+    assert np.array_equal(wm[:n].cpu().numpy(), ref_i.astype(np.int64))
+    # the same through FP64 -> fixed point -> FP64 (the Lanczos store's encoding)
+    xm, ex = E.fixed_from_f64(torch.as_tensor(xh).cuda(), p.fixed_point)
+    wm2, ew2 = p.matvec_fixed(xm, ex)
+    yf = E.fixed_to_f64(wm2, ew2)[:n].cpu().numpy()
+    np.testing.assert_allclose(yf, ref, rtol=1e-12, atol=1e-13 * np.abs(ref).max())
     gen = torch.Generator(device="cuda").manual_seed(0)
     x = torch.randn(p.dim, dtype=torch.float64, device="cuda", generator=gen)
-    y = torch.randn(p.dim, dtype=torch.float64, device="cuda", generator=gen)
-    Hx, Hy = p.matvec(x), p.matvec(y)
-    a, b = torch.dot(x, Hy).item(), torch.dot(Hx, y).item()
+    yv = torch.randn(p.dim, dtype=torch.float64, device="cuda", generator=gen)
+    Hx, Hy = p.matvec(x), p.matvec(yv)
+    a, b = torch.dot(x, Hy).item(), torch.dot(Hx, yv).item()
     assert abs(a - b) <= 1e-12 * (abs(a) + abs(b))
-    Hxy = p.matvec(2.0 * x - 3.0 * y)
+    Hxy = p.matvec(2.0 * x - 3.0 * yv)
     torch.testing.assert_close(Hxy, 2.0 * Hx - 3.0 * Hy, rtol=1e-12, atol=1e-11)
 
 
