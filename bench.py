@@ -57,27 +57,29 @@ def parse():
 
 
 def run_matvec_only(n: int):
-    """N integer matvecs of the 14-site (7,7) sector, timed with CUDA events (one JSON line)."""
+    """N fixed-point Lanczos steps of the 14-site (7,7) sector per matvec variant (5 = banded
+    two-pass sweep, 3 = single-pass), the matvec launches timed with CUDA events on the
+    launching stream (one JSON line per variant)."""
     import torch
 
     from cmpy_gb300 import engine as E
 
     bonds = [(i, j, T) for i, j in sorted(ring_bonds(N_SITES))]
     plan = E.Plan.fermion(N_SITES, [-MU] * N_SITES, [U] * N_SITES, bonds, N_UP, N_DN)
-    x = torch.rand(plan.dim, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(5))
-    xm, ex = E.fixed_from_f64(x, plan.fixed_point)
-    wm, _ = plan.matvec_fixed(xm, ex)
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * n)]
-    for k in range(n):
-        ev[2 * k].record()
-        plan.matvec_fixed(xm, ex)
-        ev[2 * k + 1].record()
-    torch.cuda.synchronize()
-    us = [ev[2 * k].elapsed_time(ev[2 * k + 1]) * 1e3 for k in range(n)]
-    mean = sum(us) / n
-    print(json.dumps({"kernel": "k_bfp_hub_matvec", "variant": os.environ.get("CMPY_ED_MATVEC", "auto"), "dim": plan.dim, "matvec_us_mean": round(mean, 2),
-                      "matvec_us_min": round(min(us), 2), "gbs": round(16.0 * plan.dim / (mean * 1e-6) / 1e9, 1)}))
+    v0 = torch.rand(plan.dim, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(5))
+    peak, _ = peaks()
+    for var in (5, 3):
+        plan.set_matvec_variant(var)
+        if plan.matvec_variant != var:
+            continue
+        E.lanczos(plan, max_steps=4, want_vector=False, v0=v0)  # warm-up
+        r = E.lanczos(plan, max_steps=n, want_vector=False, v0=v0, profile=True)
+        us = 1e3 * r.matvec_ms / max(r.matvecs, 1)
+        gbs = 16.0 * plan.dim / (us * 1e-6) / 1e9
+        print(json.dumps({"variant": var, "kernels": "k_sweep_up + k_sweep_dn" if var == 5 else "k_bfp_hub_matvec3",
+                          "dim": plan.dim, "matvecs": r.matvecs, "matvec_us": round(us, 2), "gbs": round(gbs, 1),
+                          "frac": round(gbs / peak, 4), "alpha0": float(r.alpha[0]), "energy": r.energy}), flush=True)
+    plan.set_matvec_variant(0)
 
 
 def case_gf14(steps: int = 12) -> None:
@@ -473,8 +475,8 @@ def run_disorder_batch(n_real: int = 512, n_freq: int = 1024, n_dense: int = 8):
     """Batched disorder: realisations of the 8-site Anderson-Hubbard chain (eps ~ U[-1,1],
     U=4, t=1, mu=2, n_up, n_dn ~ U{2..5}, numpy default_rng(2024)); ground state + G(w) at
     n_freq real frequencies in [-8, 8] (eta = 0.05) and 256 Matsubara points (beta = 10) each.
-    1000 Lanczos levels (no reorthogonalisation) converge the continued fractions on the real
-    axis; the accuracy is checked against dense-eigh Lehmann sums on `n_dense` realisations
+    2000 Lanczos levels (no reorthogonalisation) converge the continued fractions on the real
+    axis (1000 leave up to ~1e-6 in slowly converging realisations); the accuracy is checked against dense-eigh Lehmann sums on `n_dense` realisations
     (the largest sectors first) and against the per-realisation runs."""
     import torch
 
@@ -488,7 +490,7 @@ def run_disorder_batch(n_real: int = 512, n_freq: int = 1024, n_dense: int = 8):
     sectors = [(int(a), int(b)) for a, b in rng.integers(2, 6, size=(n_real, 2))]
     n_mats = 256
     z = np.concatenate([np.linspace(-8, 8, n_freq) + 0.05j, 1j * (2 * np.arange(n_mats) + 1) * np.pi / 10.0])
-    levels = 1000
+    levels = 2000
     for m_, s_ in zip(models, sectors):  # plans (setup, untimed)
         for d in (-1, 0, 1):
             m_.plan(s_[0] + d, s_[1])
@@ -666,73 +668,136 @@ def cpu_sample(up_rows: int):
     return csr, x, build
 
 
-def cpu_matvec_rate(csr, x, threads: int, seconds: float):
-    """H*v GB/s of the sample with `threads` row blocks in parallel (scipy releases the GIL in
-    its sparse kernels)."""
-    from concurrent.futures import ThreadPoolExecutor
-
-    n = csr.shape[0]
-    cuts = np.linspace(0, n, threads + 1).astype(int)
-    blocks = [csr[cuts[i]:cuts[i + 1]] for i in range(threads)]
-    ex = ThreadPoolExecutor(max_workers=threads)
-
-    def one():
-        list(ex.map(lambda b: b @ x, blocks))
-
-    one()
+def cpu_matvec_rate(csr, x, seconds: float):
+    """H*v GB/s of the sample on one host core (scipy's sparse product holds the GIL; this
+    process has used the GPU, so no worker processes are forked here: the all-core figure is
+    the --impl reference line)."""
+    csr @ x
     reps, t0 = 0, time.perf_counter()
     while time.perf_counter() - t0 < seconds:
-        one()
+        csr @ x
         reps += 1
     dt = (time.perf_counter() - t0) / reps
-    ex.shutdown()
-    return 16.0 * n / dt / 1e9, dt
+    return 16.0 * csr.shape[0] / dt / 1e9, dt
 
 
 def cpu_baseline_line(seconds: float = 8.0):
-    threads = os.cpu_count() or 1
     up_rows = 96
     csr, x, build = cpu_sample(up_rows)
-    gbs, dt = cpu_matvec_rate(csr, x, threads, seconds)
+    gbs, dt = cpu_matvec_rate(csr, x, seconds)
     return {
         "value": round(gbs, 4),
         "unit": "GB/s",
-        "cores": threads,
+        "cores": 1,
         "kind": "port",
         "sample": (f"reference COO (oracle restatement) of the first {up_rows} of 3432 up-rows of the 14-site (7,7) "
-                   f"sector -> scipy CSR ({csr.nnz} nnz) -> H*v over {threads} threads; COO+CSR build {build:.2f} s "
+                   f"sector -> scipy CSR ({csr.nnz} nnz) -> H*v on one core; COO+CSR build {build:.2f} s "
                    f"for the sample ({build * 3432 / up_rows:.0f} s extrapolated to the sector)"),
     }
 
 
+def _pool_csr_matvec(H, nproc: int):
+    """y = H x over `nproc` row blocks of a scipy CSR matrix in forked worker processes (scipy's
+    sparse product holds the GIL, so threads would not run in parallel). x and y live in
+    anonymous shared memory created before the fork; the blocks are sliced before the fork
+    and shared copy-on-write. Only for processes that have made no GPU call (fork).
+    Returns (matvec, close)."""
+    import mmap
+    import multiprocessing as mp
+
+    n = H.shape[0]
+    bx, by = mmap.mmap(-1, n * 8), mmap.mmap(-1, n * 8)
+    x = np.frombuffer(bx, dtype=np.float64)
+    y = np.frombuffer(by, dtype=np.float64)
+    cuts = np.linspace(0, n, nproc + 1).astype(int)
+    blocks = [H[cuts[i]:cuts[i + 1]] for i in range(nproc)]
+    ctx = mp.get_context("fork")
+
+    def worker(i, conn):
+        a, b = int(cuts[i]), int(cuts[i + 1])
+        while conn.recv():
+            y[a:b] = blocks[i] @ x
+            conn.send(1)
+
+    conns, procs = [], []
+    for i in range(nproc):
+        parent, child = ctx.Pipe()
+        pr = ctx.Process(target=worker, args=(i, child), daemon=True)
+        pr.start()
+        conns.append(parent)
+        procs.append(pr)
+
+    def mv(v):
+        x[:] = np.asarray(v, dtype=np.float64).reshape(-1)
+        for c in conns:
+            c.send(1)
+        for c in conns:
+            c.recv()
+        return y  # shared buffer: valid until the next call (eigsh copies it out at once)
+
+    def close():
+        for c in conns:
+            c.send(0)
+        for pr in procs:
+            pr.join(timeout=10)
+
+    return mv, close
+
+
 def run_reference(args, rank, world):
+    """The reference's CPU path for the 14-site (7,7) sector on this machine's host cores: the
+    reference triplets (the oracle's bit-exact restatement of cmpy/operators.py project_* and
+    cmpy/models/hubbard.py _ham_data, kind "port": the reference itself is Python that cannot
+    run here) -> scipy CSR -> eigsh(k=1, which="SA") as in cmpy/exactdiag.py:37, timed once in
+    full (gs_time_s). Each step then times `reps` full-sector CSR H*v (the operation the
+    Lanczos/ARPACK iteration repeats), row-blocked over all host threads: the line's value is
+    that H*v GB/s (16 bytes per element, as for the GPU arm)."""
     if rank != 0:
         return None
-    threads = os.cpu_count() or 1
-    up_rows = 96
-    csr, x, build = cpu_sample(up_rows)
-    from concurrent.futures import ThreadPoolExecutor
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
 
-    n = csr.shape[0]
-    cuts = np.linspace(0, n, threads + 1).astype(int)
-    blocks = [csr[cuts[i]:cuts[i + 1]] for i in range(threads)]
-    ex = ThreadPoolExecutor(max_workers=threads)
-    reps_per_step = 20
+    from oracle import ed_oracle as O
 
-    def step():
-        for _ in range(reps_per_step):
-            list(ex.map(lambda b: b @ x, blocks))
-
-    for _ in range(args.warmup):
-        step()
+    threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    up = O.sector_states(N_SITES, N_UP)
+    dn = O.sector_states(N_SITES, N_DN)
+    eps, uu, bonds, width = O.hubbard_descriptor(N_SITES, [list(b) for b in sorted(ring_bonds(N_SITES))], inter=U,
+                                                 hop=T, mu=MU)
+    D = len(up) * len(dn)
     t0 = time.perf_counter()
+    r, c, v = O.coo_fermion(up, dn, eps, uu, bonds, width)
+    n_trip = int(r.size)
+    t1 = time.perf_counter()
+    H = sp.csr_matrix((v, (r, c)), shape=(D, D))
+    del r, c, v
+    t2 = time.perf_counter()
+    mv, close = _pool_csr_matvec(H, threads)
+    count = [0]
+
+    def counted(x):
+        count[0] += 1
+        return mv(x)
+
+    op = sla.LinearOperator((D, D), matvec=counted, dtype=np.float64)
+    v0 = np.random.default_rng(0).random(D)
+    e0 = float(sla.eigsh(op, k=1, which="SA", tol=1e-12, v0=v0, return_eigenvectors=False)[0])
+    t3 = time.perf_counter()
+    x = np.random.default_rng(1).random(D)
+    reps = 4
+    for _ in range(args.warmup):
+        for _ in range(reps):
+            mv(x)
+    t4 = time.perf_counter()
     for _ in range(args.steps):
-        step()
-    el = time.perf_counter() - t0
-    ex.shutdown()
-    gbs = 16.0 * n * reps_per_step * args.steps / el / 1e9
-    D = 3432 * 3432
-    mv_s = el / (reps_per_step * args.steps) * (D / n)
+        for _ in range(reps):
+            mv(x)
+    el = time.perf_counter() - t4
+    close()
+    gbs = 16.0 * D * reps * args.steps / el / 1e9
+    sample = (f"full 14-site (7,7) sector: {n_trip} reference triplets (oracle restatement, one thread, "
+              f"{t1 - t0:.1f} s) -> scipy CSR ({H.nnz} nnz, {t2 - t1:.1f} s) -> eigsh with the CSR matvec in "
+              f"{threads} processes by row blocks ({count[0]} H*v, {t3 - t2:.1f} s); each step {reps} full-sector H*v")
     return {
         "metric": METRIC,
         "impl": "reference",
@@ -746,15 +811,55 @@ def run_reference(args, rank, world):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic",
+        "data": "synthetic (deterministic model, seeded start vector)",
         "config": {"workload": "hubbard_ring14_half_filling_gs250_cf200", "n_sites": N_SITES, "sector": [N_UP, N_DN],
-                   "dim": D, "parallelism": "host threads"},
-        "gs_time_s_extrapolated": round(250 * mv_s + build * 3432 / up_rows, 1),
-        "cpu_baseline": {"value": round(gbs, 4), "unit": "GB/s", "cores": threads, "kind": "port",
-                         "sample": f"{up_rows} of 3432 up-rows, {reps_per_step} H*v per step, scipy CSR over "
-                                   f"{threads} threads"},
+                   "dim": D, "U": U, "t": T, "mu": MU, "parallelism": f"{threads} host processes"},
+        "same_config": True,
+        "gs_time_s": round(t3 - t0, 2),
+        "gs_parts_s": {"coo_build": round(t1 - t0, 2), "csr_build": round(t2 - t1, 2), "eigsh": round(t3 - t2, 2)},
+        "gs_energy": e0,
+        "eigsh_matvecs": count[0],
+        "cpu_baseline": {"value": round(gbs, 4), "unit": "GB/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": round(gbs, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+
+
+def run_chain6():
+    """Config 1 (correctness configuration, time reported): 6-site open Hubbard chain, t=1,
+    U=4, mu=2, sector (3,3): Lanczos ground state (tol 1e-12) and the T=0 Lehmann Green's
+    function on site 0, spin up, at 512 real frequencies in [-8, 8] with eta = 0.05."""
+    import torch
+
+    from cmpy_gb300.exactdiag import gf_lehmann_zero_temperature, groundstate_sector
+    from cmpy_gb300.models import ChainLattice, HubbardModel
+
+    m = HubbardModel(ChainLattice(6), inter=4.0, mu=2.0, hop=1.0)
+    z = np.linspace(-8, 8, 512) + 0.05j
+
+    def run():
+        e0, psi = groundstate_sector(m, 3, 3, max_steps=200, tol=1e-12)
+        return e0, gf_lehmann_zero_temperature(m, z, e0, psi, 3, 3, pos=0)
+
+    run()
+    (e0, g), ms = _timed(run)
+    torch.cuda.synchronize()
+    return {"workload": "hubbard_chain6_sector33_gs_lehmann512", "ms": round(ms, 3), "gs_energy": e0,
+            "g_norm_check": float(-np.sum(g.imag) * (z[1].real - z[0].real) / np.pi)}
+
+
+def run_f64_matvec(steps: int = 20):
+    """The FP64 matvec fallback: the 14-site (7,7) ring with t = 0.7 (not a dyadic hop, so the
+    sector has no integer matvec), matvec launches timed inside an FP64 Lanczos run."""
+    from cmpy_gb300 import engine as E
+
+    bonds = [(i, j, 0.7) for i, j in sorted(ring_bonds(N_SITES))]
+    plan = E.Plan.fermion(N_SITES, [-MU] * N_SITES, [U] * N_SITES, bonds, N_UP, N_DN)
+    assert plan.fixed_point == 0
+    E.lanczos(plan, max_steps=3, want_vector=False)
+    r = E.lanczos(plan, max_steps=steps, want_vector=False, profile=True)
+    us = 1e3 * r.matvec_ms / max(r.matvecs, 1)
+    return {"workload": "hubbard_ring14_sector77_t0.7_fp64", "kernel": "k_hub_matvec_f64", "matvec_us": round(us, 2),
+            "gbs": round(16.0 * plan.dim / (us * 1e-6) / 1e9, 1)}
 
 
 def main():
@@ -788,7 +893,8 @@ def main():
             out["cpu_baseline"] = None
         if not args.no_extras and world == 1:
             for key, fn in (("batched_sweep", run_batched_sweep), ("batched_disorder", run_disorder_batch),
-                            ("adjoint", run_adjoint), ("heisenberg20", run_heisenberg)):
+                            ("adjoint", run_adjoint), ("heisenberg20", run_heisenberg), ("chain6_config1", run_chain6),
+                            ("matvec_f64_t07", run_f64_matvec)):
                 try:
                     out[key] = fn()
                 except Exception as exc:  # keep the headline line even if an extra fails

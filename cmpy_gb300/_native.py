@@ -177,6 +177,9 @@ _SIGNATURES = {
     "ed_fixed_from_f64": (I32, [P, I64, I32, P, C.POINTER(C.c_int32), P]),
     "ed_fixed_to_f64": (I32, [P, I64, C.c_int32, P, P]),
     "ed_matvec_fixed": (I32, [PLAN, P, C.c_int32, P, C.POINTER(C.c_int32), C.POINTER(I32), P]),
+    "ed_plan_matvec_variant": (I32, [PLAN]),
+    "ed_plan_set_wait_limit": (I32, [PLAN, I64]),
+    "ed_plan_set_matvec_variant": (I32, [PLAN, I32]),
     "ed_gf_continued_fraction": (I32, [P, P, I32, F64, F64, I32, P, I64, P, I32, P]),
     "ed_lehmann_accumulate": (I32, [P, I64, P, I64, P, F64, F64, P, I64, P, P]),
     "ed_tevo_sum": (I32, [P, P, I64, F64, I32, P, I64, P, I32, P]),

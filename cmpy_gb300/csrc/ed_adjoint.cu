@@ -357,7 +357,7 @@ TapeLayout tape_layout(const ed_plan_s* p, int K, int c) {
 ed_status tape_check(const ed_plan_s* p, int K, int c) {
   if (p->kind != 0) return fail(ED_ERR_INVALID_ARG, "the taped Lanczos needs a fermionic plan");
   if (p->dim < 1) return fail(ED_ERR_INVALID_ARG, "empty sector");
-  if (K < 1 || K > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  if (K < 1 || K > 4096) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 4096]");
   if (c < 1 || c > 256) return fail(ED_ERR_INVALID_ARG, "checkpoint spacing must be in [1, 256]");
   return ED_OK;
 }

@@ -495,7 +495,7 @@ ed_status bcheck(const ed_plan_s* p, int B, int K, int c) {
   if (p->kind != 0) return fail(ED_ERR_INVALID_ARG, "the batched tape needs a fermionic plan");
   if (p->dim < 1) return fail(ED_ERR_INVALID_ARG, "empty sector");
   if (B < 1 || B > 65535) return fail(ED_ERR_INVALID_ARG, "batch size must be in [1, 65535]");
-  if (K < 1 || K > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  if (K < 1 || K > 4096) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 4096]");
   if (c < 1 || c > 256) return fail(ED_ERR_INVALID_ARG, "checkpoint spacing must be in [1, 256]");
   if (p->n_sites > SW_SITES || (int)p->hop.size() > SW_BONDS)
     return fail(ED_ERR_TOO_LARGE, "batched parameters support up to 16 sites and 32 bonds");

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "ed_plan.cuh"
+#include "ed_sweep_tables.h"
 #include "ed_tridiag.cuh"
 
 namespace ed {
@@ -508,6 +509,25 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+// non-blocking test of an mbarrier phase
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// at most `limit` tests with a short sleep between them; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait_polls(uint64_t* bar, unsigned parity, long limit) {
+  for (long it = 0; it < limit; ++it) {
+    if (mbar_test(bar, parity)) return true;
+    __nanosleep(32);
+  }
+  return false;
+}
+
 // global -> shared bulk copy (16-byte aligned, size a multiple of 16), completes on `bar`
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar, uint64_t pol) {
   asm volatile(
@@ -619,7 +639,7 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
     k_bfp_hub_matvec3(BfpHubArgs a, const uint32_t* __restrict__ btab2, int n_b2, int n_b2pos, int max_up,
                       const int32_t* __restrict__ up_lst, const int32_t* __restrict__ up_cnt,
                       const int64_t* __restrict__ X, int64_t* W, double* partial,
-                      unsigned long long* partial_max, BfpState* st, int* status, BfpFuse fz) {
+                      unsigned long long* partial_max, BfpState* st, int* status, BfpFuse fz, long wait_limit) {
   if (st && *(volatile int*)&st->stop) return;
   extern __shared__ __align__(128) unsigned char sm3[];
   __shared__ double smd[MV3_MAXNT / 32];
@@ -670,7 +690,7 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
     const int s = k & 1;
     const int64_t row0 = g * MV3_R;
     const int nr = (int)min((int64_t)MV3_R, nu - row0);
-    if (mbar_wait_bounded(bar, par)) {
+    if (mbar_wait_polls(bar, par, wait_limit)) {
       pending = false;
       par ^= 1u;
     } else {
@@ -818,6 +838,8 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
     }
   }
 }
+
+#include "ed_sweep.cuh"
 
 // ---- two-pass H·v, pass 1: up-neighbour sums by column panels ---------------------------------
 // The up-hop part of H·v, W[u, c] = sum_{u'} (+-) X[u', c], is a sparse-times-dense product. A
@@ -1035,14 +1057,22 @@ __global__ void __launch_bounds__(BT, 4) k_bfp_update(BfpVecs v, int k, const in
 
 // ---- Ritz vector ------------------------------------------------------------------------------------
 // psi = sum_k C_k R_k * 2^-SC (C_k and SC from the host: see bfp_lanczos)
+// (pu, pd non-null: the vectors are in the renumbered basis of the sweep matvec and psi is
+// scattered back to the original order, nd = num_dn)
 __global__ void k_bfp_ritz(const BfpVecs v, const int64_t* __restrict__ C, const int* SCp, const BfpState* st,
-                           double* __restrict__ out) {
+                           double* __restrict__ out, const int32_t* __restrict__ pu, const int32_t* __restrict__ pd,
+                           int64_t nd) {
   const int m = st->steps;
   const int SC = *SCp;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < v.D; i += (int64_t)gridDim.x * blockDim.x) {
     I128 acc{0, 0};
     for (int k = 0; k < m; ++k) add128(acc, mul_s64(C[k], v.vec(k)[i]));
-    out[i] = ldexp(i128_to_double(acc), -SC);
+    int64_t o = i;
+    if (pu) {
+      const int64_t r = i / nd, c = i - r * nd;
+      o = (int64_t)__ldg(pu + r) * nd + __ldg(pd + c);
+    }
+    out[o] = ldexp(i128_to_double(acc), -SC);
   }
 }
 
@@ -1051,6 +1081,105 @@ __global__ void k_bfp_ritz(const BfpVecs v, const int64_t* __restrict__ C, const
 static bool is_int_scaled(double v, int F, int64_t lim) {
   const double s = std::ldexp(v, F);
   return std::isfinite(s) && s == std::floor(s) && std::fabs(s) < (double)lim;
+}
+
+// shared memory of the two sweep passes for rings of r chunks
+static size_t sweep_smem_up(int r) {
+  return (size_t)r * (SW_CH * SW_W * 8 + 8) + (size_t)SW_LR * (SW_CH * SW_LST * 2 + 8);
+}
+static size_t sweep_smem_dn(int r) {
+  return (size_t)SW_W * ((size_t)r * SW_CH + 1) * 8 + (size_t)SW_W * (SW_CH + 1) * 8 + (size_t)r * 8 +
+         (size_t)SW_LR * (SW_CH * SW_LST * 2 + 8);
+}
+
+// Tables of the banded two-pass matvec (ed_sweep.cuh); leaves B.sw.on = 0 when the sector does
+// not suit it (odd num_dn: the 16-byte bulk row copies need even rows; a target with more than
+// 15 hops; a band wider than the shared memory). CMPY_ED_SWEEP=0 disables it.
+static ed_status build_sweep(ed_plan_s* p, BfpTables& B, const std::vector<int32_t>& uoff,
+                             const std::vector<int32_t>& uidx, const std::vector<double>& ucoef,
+                             const std::vector<int32_t>& doff, const std::vector<int32_t>& didx,
+                             const std::vector<double>& dcoef, const std::vector<int32_t>& eui,
+                             const std::vector<int32_t>& edi, const std::vector<int64_t>& euf,
+                             const std::vector<int64_t>& edf, cudaStream_t s) {
+  SweepTables& W = B.sw;
+  W = SweepTables();
+  const char* env = getenv("CMPY_ED_SWEEP");
+  if (env && atoi(env) == 0) return ED_OK;
+  const int64_t nu = p->num_up, nd = p->num_dn;
+  if (nu < 1 || nd < 2 || nd % 2) return ED_OK;
+  SweepSide su, sd;
+  if (!sweep_order(nu, uoff, uidx, ucoef, &su) || !sweep_order(nd, doff, didx, dcoef, &sd)) return ED_OK;
+  // rings: as many chunks as two CTAs per SM allow (extra chunks are prefetch room), else as
+  // many as one CTA per SM allows
+  int per_sm = 0;
+  ED_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, p->device));
+  const size_t two = (size_t)per_sm / 2 - 2048, one = (size_t)p->ctx->smem_optin - 1024;
+  auto pick = [&](int need, int64_t nchunks, size_t (*smem)(int)) -> int {
+    int r2 = 0, r1 = 0;
+    while (smem(r2 + 1) <= two) ++r2;
+    while (smem(r1 + 1) <= one) ++r1;
+    const int r = need <= r2 ? r2 : (need <= r1 ? r1 : 0);
+    if (r == 0) return 0;
+    return (int)std::min<int64_t>(std::max<int64_t>(need, std::min<int64_t>(r, nchunks)), 32767 / SW_CH);
+  };
+  const int ru = pick(su.need, (nu + SW_CH - 1) / SW_CH, sweep_smem_up);
+  const int rd = pick(sd.need, (nd + SW_CH - 1) / SW_CH, sweep_smem_dn);
+  if (ru < su.need || rd < sd.need || ru == 0 || rd == 0) return ED_OK;
+  sweep_lists(nu, uoff, uidx, ucoef, ru, &su);
+  sweep_lists(nd, doff, didx, dcoef, rd, &sd);
+  // renumbered diagonal data
+  std::vector<uint64_t> st_up(nu), st_dn(nd), sup(nu), sdn(nd);
+  ED_CUDA(cudaMemcpyAsync(st_up.data(), p->up.states, nu * 8, cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(st_dn.data(), p->dn.states, nd * 8, cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  for (int64_t i = 0; i < nu; ++i) sup[i] = st_up[su.perm[i]];
+  for (int64_t i = 0; i < nd; ++i) sdn[i] = st_dn[sd.perm[i]];
+  auto up = [&](auto** dst, const void* src, size_t bytes) -> ed_status {
+    ED_CUDA(cudaMalloc((void**)dst, std::max<size_t>(bytes, 8)));
+    if (bytes) ED_CUDA(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, s));
+    return ED_OK;
+  };
+  if (!B.diag64) {
+    std::vector<int32_t> a(nu), b(nd);
+    for (int64_t i = 0; i < nu; ++i) a[i] = eui[su.perm[i]];
+    for (int64_t i = 0; i < nd; ++i) b[i] = edi[sd.perm[i]];
+    ED_TRY(up(&W.e_up, a.data(), a.size() * 4));
+    ED_TRY(up(&W.e_dn, b.data(), b.size() * 4));
+    ED_CUDA(cudaStreamSynchronize(s));
+  } else {
+    std::vector<int64_t> a(nu), b(nd);
+    for (int64_t i = 0; i < nu; ++i) a[i] = euf[su.perm[i]];
+    for (int64_t i = 0; i < nd; ++i) b[i] = edf[sd.perm[i]];
+    ED_TRY(up(&W.f_up, a.data(), a.size() * 8));
+    ED_TRY(up(&W.f_dn, b.data(), b.size() * 8));
+    ED_CUDA(cudaStreamSynchronize(s));
+  }
+  ED_TRY(up(&W.perm_up, su.perm.data(), su.perm.size() * 4));
+  ED_TRY(up(&W.perm_dn, sd.perm.data(), sd.perm.size() * 4));
+  ED_TRY(up(&W.lst_up, su.lst.data(), su.lst.size() * 2));
+  ED_TRY(up(&W.lst_dn, sd.lst.data(), sd.lst.size() * 2));
+  ED_TRY(up(&W.win_up, su.win.data(), su.win.size() * sizeof(int2)));
+  ED_TRY(up(&W.win_dn, sd.win.data(), sd.win.size() * sizeof(int2)));
+  ED_TRY(up(&W.s_up, sup.data(), sup.size() * 8));
+  ED_TRY(up(&W.s_dn, sdn.data(), sdn.size() * 8));
+  ED_CUDA(cudaStreamSynchronize(s));
+  W.ring_up = ru;
+  W.ring_dn = rd;
+  W.nblk_up = (int)su.win.size();
+  W.nblk_dn = (int)sd.win.size();
+  // L2 policies (bit set = evict_last): pass 1 X loads, pass 1 S stores, pass 2 X loads, pass 2
+  // W stores; default keeps S for pass 2 and W for the update kernel
+  const char* pe = getenv("CMPY_ED_SWEEP_POL");
+  W.pol = pe ? atoi(pe) : 0b1010;
+  W.on = 1;
+  return ED_OK;
+}
+
+static void free_sweep(SweepTables& W) {
+  cudaFree(W.perm_up); cudaFree(W.perm_dn); cudaFree(W.lst_up); cudaFree(W.lst_dn);
+  cudaFree(W.win_up); cudaFree(W.win_dn); cudaFree(W.s_up); cudaFree(W.s_dn);
+  cudaFree(W.e_up); cudaFree(W.e_dn); cudaFree(W.f_up); cudaFree(W.f_dn);
+  W = SweepTables();
 }
 
 ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
@@ -1258,6 +1387,7 @@ ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
     ED_TRY(up(&B.e_dn_fx, edf.data(), edf.size() * 8));
   }
   ED_CUDA(cudaStreamSynchronize(s));
+  ED_TRY(build_sweep(p, B, uoff, uidx, ucoef, doff, didx, dcoef, eui, edi, euf, edf, s));
   B.eligible = 1;
   return ED_OK;
 }
@@ -1267,8 +1397,12 @@ void free_bfp(ed_plan_s* p) {
   cudaFree(B.up_off); cudaFree(B.up_npos); cudaFree(B.up_idx); cudaFree(B.dn_tab); cudaFree(B.dn_btab2);
   cudaFree(B.up_lst); cudaFree(B.up_cnt);
   cudaFree(B.e_up_int); cudaFree(B.e_dn_int); cudaFree(B.e_up_fx); cudaFree(B.e_dn_fx);
+  free_sweep(B.sw);
   B = BfpTables();
 }
+
+// first-wait limit of the bulk-copy matvecs (polls); 0 selects MV3_WAIT_LIMIT
+static long wait_limit(const ed_plan_s* p) { return p->bfp.wait_limit > 0 ? p->bfp.wait_limit : MV3_WAIT_LIMIT; }
 
 static BfpHubArgs bfp_args(const ed_plan_s* p) {
   const BfpTables& B = p->bfp;
@@ -1307,15 +1441,18 @@ static int v3_threads(const ed_plan_s* p) {
   return (int)std::min<int64_t>(MV3_MAXNT, 32 * std::max<int64_t>(1, warps));
 }
 
-// matvec variant: 3 (bulk-copied double-buffered rows, bond-major dn table) when both stages and
-// the table fit in shared memory, else 2 (resident slot table, one stage), else 1. Rows must
-// have an even length (16-byte row copies). CMPY_ED_MATVEC=1|2|3 forces a variant when possible.
+// matvec variant: 5 (banded two-pass sweep in the renumbered basis, ed_sweep.cuh) when the
+// plan has its tables, else 3 (bulk-copied double-buffered rows, bond-major dn table) when both
+// stages and the table fit in shared memory, else 2 (resident slot table, one stage), else 1.
+// Rows must have an even length (16-byte row copies). CMPY_ED_MATVEC=1|2|3|4|5 forces a
+// variant when possible.
 static int matvec_variant(const ed_plan_s* p) {
-  static int forced = -1;
-  if (forced < 0) {
+  static int env_forced = -1;
+  if (env_forced < 0) {
     const char* e = getenv("CMPY_ED_MATVEC");
-    forced = e ? atoi(e) : 0;
+    env_forced = e ? atoi(e) : 0;
   }
+  const int forced = p->bfp.force_var > 0 ? p->bfp.force_var : env_forced;
   const size_t optin = (size_t)p->ctx->smem_optin;
   const bool v2_ok = p->bfp.vec2 && v2_smem(p) + MV2_STATIC_SMEM <= optin && p->num_up >= 1;
   // list entries are int32 element offsets u * nd: the vector must have fewer than 2^31 elements
@@ -1325,14 +1462,18 @@ static int matvec_variant(const ed_plan_s* p) {
                      p->dim < ((int64_t)1 << 31) && p->num_dn < 4096;
   // two-pass (4): column panels of 4 (nd % 4 == 0), a panel of all rows in half the shared memory
   const bool v4_ok = v3_ok && p->num_dn % MV_PW == 0 && (size_t)p->num_up * MV_PW * 8 + 1024 <= optin / 2;
+  const bool v5_ok = p->bfp.sw.on != 0;
   if (forced == 1) return 1;
   if (forced == 2) return v2_ok ? 2 : 1;
+  if (forced == 3 && v3_ok) return 3;
   if (forced == 4 && v4_ok) return 4;  // measured slower than 3 on GB300 (kept for comparison)
+  if (v5_ok && (forced == 0 || forced == 5)) return 5;
   if (v3_ok) return 3;
   return v2_ok ? 2 : 1;
 }
 
 static int bfp_matvec_grid(const ed_plan_s* p) {
+  if (matvec_variant(p) == 5) return (int)((p->num_up + SW_W - 1) / SW_W);  // pass 2 writes the partials
   if (matvec_variant(p) >= 3)
     return (int)std::min<int64_t>((p->num_up + MV3_R - 1) / MV3_R, (int64_t)p->ctx->num_sms);
   if (matvec_variant(p) == 2)
@@ -1387,8 +1528,38 @@ static ed_status launch_v3(const ed_plan_s* p, int g, const int64_t* X, int64_t*
   }
   k_bfp_hub_matvec3<DIAG64, UPW><<<g, v3_threads(p), v3_smem(p), s>>>(bfp_args(p), B.dn_btab2, B.n_b2, B.n_b2pos,
                                                                       B.max_up, B.up_lst, B.up_cnt, X, W, partial,
-                                                                      partial_max, st, status, fz);
+                                                                      partial_max, st, status, fz, wait_limit(p));
   ED_CHECK_LAUNCH("k_bfp_hub_matvec3");
+  return ED_OK;
+}
+
+// the two sweep passes on renumbered vectors: S = A X into W, then W = t (S + X B) + D X with
+// the Lanczos partials (and the step's scalars when fz.on)
+template <bool DIAG64>
+static ed_status launch_sweep(const ed_plan_s* p, const int64_t* X, int64_t* W, double* partial,
+                              unsigned long long* partial_max, BfpState* st, cudaStream_t s, const BfpFuse& fz) {
+  static std::atomic<uint64_t> done{0};
+  const uint64_t bit = 1ull << (p->device & 63);
+  if (!(done.load() & bit)) {
+    cudaFuncAttributes fa;
+    ED_CUDA(cudaFuncGetAttributes(&fa, k_sweep_up));
+    ED_CUDA(cudaFuncSetAttribute(k_sweep_up, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 p->ctx->smem_optin - (int)fa.sharedSizeBytes));
+    ED_CUDA(cudaFuncGetAttributes(&fa, k_sweep_dn<DIAG64>));
+    ED_CUDA(cudaFuncSetAttribute(k_sweep_dn<DIAG64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 p->ctx->smem_optin - (int)fa.sharedSizeBytes));
+    done.fetch_or(bit);
+  }
+  const SweepTables& w = p->bfp.sw;
+  int* status = st ? &st->status : p->ctx->d_status;
+  const int64_t nu = p->num_up, nd = p->num_dn;
+  SweepArgs au{nu, nd, w.ring_up, w.nblk_up, w.lst_up, w.win_up, w.pol & 3, wait_limit(p)};
+  k_sweep_up<<<(int)((nd + SW_W - 1) / SW_W), SW_NT, sweep_smem_up(w.ring_up), s>>>(au, X, W, st, status);
+  SweepArgs ad{nu, nd, w.ring_dn, w.nblk_dn, w.lst_dn, w.win_dn, (w.pol >> 2) & 3, wait_limit(p)};
+  const SweepDiag dg{w.s_up, w.s_dn, w.e_up, w.e_dn, w.f_up, w.f_dn};
+  k_sweep_dn<DIAG64><<<(int)((nu + SW_W - 1) / SW_W), SW_NT, sweep_smem_dn(w.ring_dn), s>>>(
+      bfp_args(p), ad, dg, X, W, partial, partial_max, st, status, fz);
+  ED_CHECK_LAUNCH_N("sweep matvec", 2);
   return ED_OK;
 }
 
@@ -1424,6 +1595,13 @@ static ed_status launch_bfp_matvec(const ed_plan_s* p, const int64_t* X, int64_t
   // caller buffers take the one-column v1 kernel
   const bool aligned = (((uintptr_t)X | (uintptr_t)W) & 15) == 0;
   const int var = aligned ? matvec_variant(p) : 1;
+  if (var == 5) {
+    // renumbered vectors (the callers that choose variant 5 convert in and out)
+    const BfpFuse& f = (fz && partial && st) ? *fz : off;
+    if (fused) *fused = f.on != 0;
+    return p->bfp.diag64 ? launch_sweep<true>(p, X, W, partial, partial_max, st, s, f)
+                         : launch_sweep<false>(p, X, W, partial, partial_max, st, s, f);
+  }
   if (var >= 3) {
     const BfpFuse& f = (fz && partial && st) ? *fz : off;
     if (fused) *fused = f.on != 0;
@@ -1506,13 +1684,19 @@ static BfpRun bfp_bind(const ed_plan_s* p, void* work, int K, bool store) {
 }
 
 // start vector (FP64, device) -> R_0 in BFP, beta_0 = ||v0||
-static ed_status bfp_start(const ed_plan_s* p, BfpRun& r, const double* v0, double* beta, cudaStream_t s) {
+// (renum: the run uses the sweep matvec, R_0 is stored in its renumbered basis)
+static ed_status bfp_start(const ed_plan_s* p, BfpRun& r, const double* v0, double* beta, cudaStream_t s,
+                           bool renum) {
   const int64_t D = p->dim;
   const int gs = grid_for(D, 256, p->ctx->num_sms * 8);
   unsigned long long* mxb = (unsigned long long*)(r.misc + 8);
   ED_CUDA(cudaMemsetAsync(mxb, 0, 8, s));
   k_maxabs_f64<<<gs, BT, 0, s>>>(v0, D, mxb);
-  k_f64_to_bfp<<<gs, 256, 0, s>>>(v0, D, mxb, p->bfp.m_in, r.v.vec(0), r.v.eR, r.v.maxR);
+  if (renum)
+    k_f64_to_bfp_perm<<<gs, 256, 0, s>>>(v0, p->num_up, p->num_dn, p->bfp.sw.perm_up, p->bfp.sw.perm_dn, mxb,
+                                         p->bfp.m_in, r.v.vec(0), r.v.eR, r.v.maxR);
+  else
+    k_f64_to_bfp<<<gs, 256, 0, s>>>(v0, D, mxb, p->bfp.m_in, r.v.vec(0), r.v.eR, r.v.maxR);
   k_bfp_norm<<<r.L.nparts, BT, 0, s>>>(r.v, 0, r.part, r.st, beta);
   ED_CHECK_LAUNCH_N("bfp start", 3);
   unsigned long long hm = 0;
@@ -1575,10 +1759,11 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
   const int64_t D = p->dim;
   const bool store = prm->want_vector != 0;
   BfpRun r = bfp_bind(p, work, K, store);
+  const bool renum = matvec_variant(p) == 5;
   ED_CUDA(cudaMemsetAsync(r.st, 0, sizeof(BfpState), s));
   ED_CUDA(cudaMemsetAsync(alpha, 0, K * sizeof(double), s));
   ED_CUDA(cudaMemsetAsync(beta, 0, (K + 1) * sizeof(double), s));
-  ED_TRY(bfp_start(p, r, v0_dev, beta, s));
+  ED_TRY(bfp_start(p, r, v0_dev, beta, s, renum));
   const int Km = (int)std::min<int64_t>(K, D);
   std::vector<cudaEvent_t> ev;
   if (prm->profile) {
@@ -1640,7 +1825,9 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
     ED_CUDA(cudaMemcpyAsync(r.C, hC.data(), m * sizeof(int64_t), cudaMemcpyHostToDevice, s));
     ED_CUDA(cudaMemcpyAsync(r.misc, &SC, sizeof(int), cudaMemcpyHostToDevice, s));
     ED_CUDA(cudaMemcpyAsync(&r.st->steps, &m, sizeof(int), cudaMemcpyHostToDevice, s));
-    k_bfp_ritz<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(r.v, r.C, r.misc, r.st, evec);
+    k_bfp_ritz<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(
+        r.v, r.C, r.misc, r.st, evec, renum ? p->bfp.sw.perm_up : nullptr, renum ? p->bfp.sw.perm_dn : nullptr,
+        p->num_dn);
     ED_CHECK_LAUNCH("k_bfp_ritz");
     ED_CUDA(cudaStreamSynchronize(s));  // the host arrays above are sources of the copies
   }
@@ -1685,7 +1872,7 @@ ed_status bfp_lanczos_coeffs(const ed_plan_s* p, int K, const double* start, voi
     if (!std::isfinite(mx)) return fail(ED_ERR_NONFINITE, "start vector is not finite");
     if (mx == 0.0) { *steps = 0; *norm = 0.0; return ED_OK; }
   }
-  ED_TRY(bfp_start(p, r, start, beta, s));
+  ED_TRY(bfp_start(p, r, start, beta, s, matvec_variant(p) == 5));
   const int Km = (int)std::min<int64_t>(K, D);
   for (int k = 0; k < Km; ++k) ED_TRY(bfp_step(p, r, k, alpha, beta, s));
   BfpState hs;
@@ -1756,7 +1943,40 @@ ED_API ed_status ed_matvec_fixed(ed_plan p, const int64_t* d_xm, int32_t ex, int
   if (p->dim == 0) return ED_OK;
   if (!d_xm || !d_wm) return fail(ED_ERR_INVALID_ARG, "null vector");
   if (d_xm == d_wm) return fail(ED_ERR_INVALID_ARG, "x and w must not alias");
-  return launch_bfp_matvec(p, d_xm, d_wm, nullptr, nullptr, nullptr, as_stream(stream));
+  cudaStream_t s = as_stream(stream);
+  if ((((uintptr_t)d_xm | (uintptr_t)d_wm) & 15) == 0 && matvec_variant(p) == 5) {
+    // the sweep matvec works in its renumbered basis: renumber x, apply, renumber back
+    int64_t* tmp = nullptr;
+    ED_CUDA(cudaMallocAsync((void**)&tmp, 2 * (size_t)p->dim * sizeof(int64_t), s));
+    const int g = grid_for(p->dim, 256, p->ctx->num_sms * 8);
+    const SweepTables& w = p->bfp.sw;
+    k_sweep_permute<<<g, 256, 0, s>>>(d_xm, tmp, p->num_up, p->num_dn, w.perm_up, w.perm_dn, 1);
+    ED_CHECK_LAUNCH("k_sweep_permute");
+    ed_status st = launch_bfp_matvec(p, tmp, tmp + p->dim, nullptr, nullptr, nullptr, s);
+    if (st == ED_OK) {
+      k_sweep_permute<<<g, 256, 0, s>>>(tmp + p->dim, d_wm, p->num_up, p->num_dn, w.perm_up, w.perm_dn, 0);
+      ED_CHECK_LAUNCH("k_sweep_permute");
+    }
+    ED_CUDA(cudaFreeAsync(tmp, s));
+    return st;
+  }
+  return launch_bfp_matvec(p, d_xm, d_wm, nullptr, nullptr, nullptr, s);
+}
+
+ED_API ed_status ed_plan_set_wait_limit(ed_plan p, int64_t polls) {
+  ED_TRY(check_plan(p));
+  if (polls < 0) return fail(ED_ERR_INVALID_ARG, "polls must be >= 0");
+  p->bfp.wait_limit = (long)polls;
+  return ED_OK;
+}
+
+ED_API int ed_plan_matvec_variant(ed_plan p) { return (p && p->bfp.eligible) ? matvec_variant(p) : 0; }
+
+ED_API ed_status ed_plan_set_matvec_variant(ed_plan p, int variant) {
+  ED_TRY(check_plan(p));
+  if (variant < 0 || variant > 5) return fail(ED_ERR_INVALID_ARG, "variant must be in [0, 5]");
+  p->bfp.force_var = variant;
+  return ED_OK;
 }
 
 ED_API int ed_plan_fixed_point(ed_plan p) { return (p && p->bfp.eligible) ? p->bfp.m_in : 0; }

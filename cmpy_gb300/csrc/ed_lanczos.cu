@@ -366,7 +366,7 @@ static ed_status use_fixed(const ed_plan_s* p, const ed_lanczos_params* prm, boo
 ED_API ed_status ed_lanczos_workspace(ed_plan p, const ed_lanczos_params* prm, size_t* bytes) {
   ED_TRY(check_plan(p));
   if (!prm || !bytes) return fail(ED_ERR_INVALID_ARG, "null argument");
-  if (prm->max_steps < 1 || prm->max_steps > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  if (prm->max_steps < 1 || prm->max_steps > 4096) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 4096]");
   bool fixed = false;
   ED_TRY(use_fixed(p, prm, &fixed));
   const bool store = prm->want_vector || prm->reorth;
@@ -390,7 +390,7 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
   ED_TRY(check_plan(p));
   if (!prm || !res || !d_alpha || !d_beta) return fail(ED_ERR_INVALID_ARG, "null argument");
   const int K = prm->max_steps;
-  if (K < 1 || K > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  if (K < 1 || K > 4096) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 4096]");
   const int64_t D = p->dim;
   if (D < 1) return fail(ED_ERR_INVALID_ARG, "empty sector");
   if (prm->want_vector && !d_evec) return fail(ED_ERR_INVALID_ARG, "want_vector needs d_evec");
@@ -563,7 +563,7 @@ ED_API ed_status ed_lanczos_coeffs(ed_plan p, int K, const double* d_start, void
                                    double* d_alpha, double* d_beta, int* h_steps, double* h_norm, ed_stream_t stream) {
   ED_TRY(check_plan(p));
   if (!d_start || !d_alpha || !d_beta || !h_steps || !h_norm) return fail(ED_ERR_INVALID_ARG, "null argument");
-  if (K < 1 || K > 1000) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 1000]");
+  if (K < 1 || K > 4096) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 4096]");
   const int64_t D = p->dim;
   if (D < 1) return fail(ED_ERR_INVALID_ARG, "empty sector");
   if (p->bfp.eligible) {

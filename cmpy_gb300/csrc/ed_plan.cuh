@@ -33,6 +33,31 @@ struct FermionParams {
   double u[ED_MAX_SITES + 2];
 };
 
+// Tables of the banded two-pass ("sweep") fixed-point matvec (ed_sweep.cuh). The up and the
+// dn states are renumbered (reverse Cuthill-McKee order of each spin's hop graph) so that the
+// single-spin hop matrices are banded; a Lanczos run that uses this matvec keeps its vectors
+// in the renumbered basis (index u' * num_dn + d').
+struct SweepTables {
+  int on = 0;
+  int ring_up = 0, ring_dn = 0;  // ring capacity in chunks of 32 rows (pass 1) / 32 columns (pass 2)
+  int nblk_up = 0, nblk_dn = 0;  // target blocks of 32 rows / 32 columns
+  int32_t* perm_up = nullptr;    // [nu] renumbered -> original up index
+  int32_t* perm_dn = nullptr;    // [nd]
+  // hop lists per renumbered target, 16 uint16 each: entries (ring offset | 0x8000 for a
+  // negative sign), entry 15 = count
+  uint16_t* lst_up = nullptr;    // [nu][16]
+  uint16_t* lst_dn = nullptr;    // [nd][16]
+  int2* win_up = nullptr;        // [nblk_up] (first chunk still needed, last chunk needed)
+  int2* win_dn = nullptr;        // [nblk_dn]
+  uint64_t* s_up = nullptr;      // states, renumbered
+  uint64_t* s_dn = nullptr;
+  int32_t* e_up = nullptr;       // diagonal mode 0 energies, renumbered
+  int32_t* e_dn = nullptr;
+  int64_t* f_up = nullptr;       // diagonal mode 1 energies, renumbered
+  int64_t* f_dn = nullptr;
+  int pol = 0;                   // L2 policy selection of the two passes (see ed_sweep.cuh)
+};
+
 // Tables of the block-fixed-point (BFP) matvec. Eligible sectors have one hopping magnitude
 // |t| = t_int * 2^-F (t_int a small integer). Output exponent e_w = e_x - F and
 //   W = t_int * sum(+-X_nbr) + D(X)
@@ -78,6 +103,9 @@ struct BfpTables {
   int up_lstride = 0;
   int32_t* e_up_int = nullptr;  // [nu]
   int32_t* e_dn_int = nullptr;  // [nd]
+  SweepTables sw;
+  long wait_limit = 0;          // polls of a first bulk-copy wait before giving up (0: default)
+  int force_var = 0;            // matvec variant chosen for this plan (0: automatic)
 };
 
 }  // namespace ed

@@ -224,6 +224,21 @@ class Plan:
         """Input mantissa bits of the sector's integer matvec, 0 if it has none."""
         return int(N.lib().ed_plan_fixed_point(self._h))
 
+    @property
+    def matvec_variant(self) -> int:
+        """Fixed-point matvec the plan uses: 5 = banded two-pass sweep (renumbered basis inside
+        the Lanczos), 3/2/1 = single-pass kernels, 0 = none (FP64 matvec)."""
+        return int(N.lib().ed_plan_matvec_variant(self._h))
+
+    def set_matvec_variant(self, variant: int) -> None:
+        """Choose the fixed-point matvec variant (0 = automatic) for comparisons and timing."""
+        N.check(N.lib().ed_plan_set_matvec_variant(self._h, int(variant)))
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Polls of a first bulk-copy wait in the fixed-point matvec before it gives up and the
+        solve reports ED_ERR_TIMEOUT (0 = default)."""
+        N.check(N.lib().ed_plan_set_wait_limit(self._h, int(polls)))
+
     def matvec_fixed(self, xm: torch.Tensor, ex: int) -> tuple[torch.Tensor, int]:
         """Exact integer H*x for x = xm * 2^ex (int64 mantissas); returns (wm, ew)."""
         with self._dev():

@@ -440,6 +440,20 @@ ED_API ed_status ed_fixed_to_f64(const int64_t* d_xm, int64_t n, int32_t exp, do
  * ed_plan_fixed_point, also returned in *h_m_in), output exponent *h_ew = ex - F. */
 ED_API ed_status ed_matvec_fixed(ed_plan plan, const int64_t* d_xm, int32_t ex, int64_t* d_wm,
                                  int32_t* h_ew, int* h_m_in, ed_stream_t stream);
+/* Which fixed-point matvec the plan uses (0: none). 5 is the banded two-pass sweep: the plan
+ * renumbers the up and the dn states (reverse Cuthill-McKee order of each spin's hop graph)
+ * and its Lanczos runs keep their vectors in that basis; ed_matvec_fixed still takes and
+ * returns vectors in the sector's ascending-state order. 3, 2, 1: single-pass kernels. The
+ * environment variable CMPY_ED_MATVEC=1..5 forces a variant where the sector allows it. */
+ED_API int ed_plan_matvec_variant(ed_plan plan);
+/* Chooses the fixed-point matvec variant of this plan (0: automatic, 1..5 as above when the
+ * sector allows it, else the automatic choice); for comparisons and benchmarks. Takes effect
+ * for the next call; not while a Lanczos run of the plan is in flight. */
+ED_API ed_status ed_plan_set_matvec_variant(ed_plan plan, int variant);
+/* Polls of a first wait for a bulk copy in the fixed-point matvec before the kernel gives up
+ * (records ED_ERR_TIMEOUT in the solve, lets its copies land and returns); 0 restores the
+ * default (2^22 polls). A small limit lets tests exercise the give-up path. */
+ED_API ed_status ed_plan_set_wait_limit(ed_plan plan, int64_t polls);
 
 /* Allocation-free ed_tridiag_lowest (no counterpart in the reference). For callers that
  * cannot allocate device memory where they need the result: hosts whose device memory

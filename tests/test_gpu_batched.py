@@ -89,7 +89,7 @@ def test_batched_vectors_and_configs(cuda):
 
 def test_batched_gf_vs_dense(cuda):
     """Realisations of the 8-site Anderson-Hubbard chain (eps ~ U[-1,1], U=4, t=1, mu=2),
-    sectors up to (4,4) (target sectors of dimension 3,920): with 1000 Lanczos levels the
+    sectors up to (4,4) (target sectors of dimension 3,920): with 2000 Lanczos levels the
     batched continued fractions equal the dense-eigh Lehmann sum to 1e-8 on the real axis
     (eta = 0.05) and on the Matsubara axis, and equal the per-realisation runs to 1e-8."""
     from cmpy_gb300.batched import greens_functions_batched
@@ -101,7 +101,7 @@ def test_batched_gf_vs_dense(cuda):
     models = [_hub(n, False, inter=4.0, eps=rng.uniform(-1, 1, n), mu=2.0) for _ in sectors]
     nw = 256
     z = np.concatenate([np.linspace(-8, 8, nw) + 0.05j, 1j * (2 * np.arange(64) + 1) * np.pi / 10.0])
-    levels = 1000
+    levels = 2000
     e, g = greens_functions_batched(models, sectors, z, gf_levels=levels)
     g = g.cpu().numpy()
     for i, (m, (nu, nd)) in enumerate(zip(models, sectors)):
