@@ -142,6 +142,8 @@ _SIGNATURES = {
     "ed_lanczos_coeffs": (I32, [PLAN, I32, P, P, C.c_size_t, P, P, C.POINTER(I32), C.POINTER(F64), P]),
     "ed_tridiag_lowest": (I32, [P, P, I32, P, P, P]),
     "ed_tridiag_lowest_noalloc": (I32, [P, P, I32, P, P, P]),
+    "ed_tridiag_lowest_batch": (I32, [P, I32, P, I32, P, I32, I32, P, P, I32, P]),
+    "ed_tridiag_pinv_solve_batch": (I32, [P, I32, P, I32, P, I32, I32, P, P, I32, P, P, I32, P]),
     "ed_batch_create": (I32, [C.POINTER(C.c_void_p), I32, C.POINTER(C.c_void_p)]),
     "ed_batch_destroy": (I32, [C.c_void_p]),
     "ed_batch_workspace": (I32, [C.c_void_p, I32, I32, I32, I32, C.POINTER(C.c_size_t)]),

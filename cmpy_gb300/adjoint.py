@@ -23,7 +23,8 @@ Backward (exact reverse of the computed recurrences):
     theta_bar += wbar_k^T (dH/dtheta) q_k (fused into the step's elementwise kernel) and
     qbar_k += H wbar_k;
   * Ritz vector and tridiagonal eigenpair: Tbar = Ebar c c^T + v c^T, v = -(T - E0)^+ cbar
-    (an m x m problem, solved on the host).
+    (the eigenpair and this m x m solve run on the device, ed_tridiag_lowest_batch and
+    ed_tridiag_pinv_solve_batch).
 Costs: forward = m0 + m_p + m_h matvecs; backward = one matvec per step for the segment
 recompute plus one for H wbar, i.e. about 2x the forward.
 """
@@ -158,17 +159,6 @@ def cf_adjoint(alpha: torch.Tensor, beta: torch.Tensor, n2: float, z: torch.Tens
     return abar, bbar, scal[0]
 
 
-def _tridiag_lowest_host(a: np.ndarray, b: np.ndarray):
-    """Lowest eigenpair of the tridiagonal (a[0..m), b[1..m)), LAPACK on the host."""
-    from scipy.linalg import eigh_tridiagonal
-
-    m = a.size
-    if m == 1:
-        return float(a[0]), np.ones(1)
-    w, v = eigh_tridiagonal(a, b[1:m], select="i", select_range=(0, 0))
-    return float(w[0]), v[:, 0]
-
-
 # ------------------------------------------------------------------------------------------
 # the autograd function
 # ------------------------------------------------------------------------------------------
@@ -182,10 +172,10 @@ def _gf_forward(theta: torch.Tensor, spec, zt: torch.Tensor, g: torch.Tensor):
     gen = torch.Generator(device="cpu").manual_seed(seed)
     v0 = torch.rand(plan.dim, generator=gen, dtype=torch.float64).to(E.device())
     tape0 = tape_forward(plan, v0, m0, c, tol=1e-12)
-    a_h = tape0.alpha.cpu().numpy()
-    b_h = tape0.beta.cpu().numpy()
-    e0, cvec_h = _tridiag_lowest_host(a_h, b_h)
-    cvec = torch.as_tensor(cvec_h, dtype=torch.float64).to(E.device())
+    m = tape0.m
+    e0_d, vecs = E.tridiag_lowest_batch(tape0.alpha[None, :m], tape0.beta[None, :m + 1], [m])
+    e0 = float(e0_d[0])
+    cvec = vecs[0, :m].contiguous()
     y, _ = tape_combine(tape0, coef=cvec)
     ynorm = torch.linalg.norm(y)
     psi = y / ynorm
@@ -204,12 +194,12 @@ def _gf_forward(theta: torch.Tensor, spec, zt: torch.Tensor, g: torch.Tensor):
         n2 = float(tape.beta[0].item()) ** 2
         E.continued_fraction(tape.alpha, tape.beta, n2, zt, e0, sign, out=g)
         parts.append((tp, tape, sign, create, n2))
-    return (plan, tape0, a_h, b_h, cvec_h, e0, ynorm, psi, zt, parts, spec)
+    return (plan, tape0, e0_d, cvec, e0, ynorm, psi, zt, parts, spec)
 
 
 def _gf_backward(saved, gbar: torch.Tensor) -> torch.Tensor:
     """Backward of one problem on the current stream: dL/dtheta for L = Re sum conj(gbar) G."""
-    plan, tape0, a_h, b_h, cvec, e0, ynorm, psi, zt, parts, spec = saved
+    plan, tape0, e0_d, cvec, e0, ynorm, psi, zt, parts, spec = saved
     n_sites, bonds, width, (nu, nd), pos, sigma, m0, mgf, c, seed = spec
     P = 2 * n_sites + len(bonds)
     theta_bar = torch.zeros(P, dtype=torch.float64, device=E.device())
@@ -228,21 +218,17 @@ def _gf_backward(saved, gbar: torch.Tensor) -> torch.Tensor:
     # psi = y / ||y||, y = sum_k c_k q_k
     ybar = (psibar - torch.dot(psibar, psi) * psi) / ynorm
     m = tape0.m
-    _, cbar_d = tape_combine(tape0, probe=ybar)
-    cbar = cbar_d.cpu().numpy()
+    _, cbar = tape_combine(tape0, probe=ybar)
     # eigenpair of T: E0 = c^T T c, c = ground state of T; v = -(T - E0)^+ cbar on the
-    # complement of c (c c^T added to make the system regular)
-    T = np.diag(a_h) + np.diag(b_h[1:m], 1) + np.diag(b_h[1:m], -1)
-    cb = cbar - np.dot(cbar, cvec) * cvec
-    v = -np.linalg.solve(T - e0 * np.eye(m) + np.outer(cvec, cvec), cb)
-    v = v - np.dot(v, cvec) * cvec
+    # complement of c (device solve)
+    v = E.tridiag_pinv_solve_batch(tape0.alpha[None, :m], tape0.beta[None, :m + 1], [m], e0_d, cvec[None],
+                                   cbar[None, :m].contiguous())[0]
+    dev = E.device()
     abar0 = e0bar * cvec ** 2 + v * cvec
-    bbar0 = np.zeros(m + 1)
+    bbar0 = torch.zeros(m + 1, dtype=torch.float64, device=dev)
     if m > 1:
         bbar0[1:m] = 2.0 * e0bar * cvec[:-1] * cvec[1:] + v[:-1] * cvec[1:] + v[1:] * cvec[:-1]
-    dev = E.device()
-    tape_reverse(tape0, torch.as_tensor(abar0).to(dev), torch.as_tensor(bbar0).to(dev), theta_bar,
-                 ext_coef=torch.as_tensor(cvec).to(dev), ext_vec=ybar)
+    tape_reverse(tape0, abar0.contiguous(), bbar0, theta_bar, ext_coef=cvec, ext_vec=ybar)
     return theta_bar
 
 
@@ -408,14 +394,8 @@ def _gf_forward_batch(thetas: torch.Tensor, spec, zt: torch.Tensor, g: torch.Ten
     gen = torch.Generator(device="cpu").manual_seed(seed)
     v0 = torch.rand(plan.dim, generator=gen, dtype=torch.float64).to(dev)
     tape0 = batch_tape_forward(plan, th, diag, v0.expand(B, -1), m0, c, tol=1e-12)
-    a_h = tape0.alpha.cpu().numpy()
-    b_h = tape0.beta.cpu().numpy()
-    e0 = np.zeros(B)
-    cv = np.zeros((B, tape0.K))
-    for b in range(B):
-        m = tape0.m[b]
-        e0[b], cv[b, :m] = _tridiag_lowest_host(a_h[b, :m], b_h[b, :m + 1])
-    cvec = torch.as_tensor(cv).to(dev)
+    e0_d, cvec = E.tridiag_lowest_batch(tape0.alpha, tape0.beta, tape0.m)
+    e0 = e0_d.cpu().numpy()
     Y, _ = batch_tape_combine(tape0, coef=cvec)
     ynorm = torch.linalg.norm(Y, dim=1)
     psi = Y / ynorm[:, None]
@@ -431,11 +411,11 @@ def _gf_forward_batch(thetas: torch.Tensor, spec, zt: torch.Tensor, g: torch.Ten
         n2 = tape.beta[:, 0].cpu().numpy() ** 2
         batch_cf(tape, n2, e0, sign, zt, g)
         parts.append((tp, tape, sign, create, n2))
-    return (plan, tape0, a_h, b_h, cv, e0, ynorm, psi, zt, parts, spec)
+    return (plan, tape0, e0_d, cvec, e0, ynorm, psi, zt, parts, spec)
 
 
 def _gf_backward_batch(saved, gbar: torch.Tensor) -> torch.Tensor:
-    plan, tape0, a_h, b_h, cv, e0, ynorm, psi, zt, parts, spec = saved
+    plan, tape0, e0_d, cv, e0, ynorm, psi, zt, parts, spec = saved
     n_sites, bonds = spec[0], spec[1]
     B = psi.shape[0]
     dev = E.device()
@@ -454,33 +434,20 @@ def _gf_backward_batch(saved, gbar: torch.Tensor) -> torch.Tensor:
         sbar = batch_tape_reverse(tape, Ab, Bb, theta_bar)
         psibar = psibar + _apply_fermion_rows(tp, plan, pos, sigma, not create, sbar)
     ybar = (psibar - torch.sum(psibar * psi, dim=1, keepdim=True) * psi) / ynorm[:, None]
-    _, cbar_d = batch_tape_combine(tape0, probe=ybar)
-    cbar = cbar_d.cpu().numpy()
-    eb_h = e0bar.cpu().numpy()
-    # v_b = -(T_b - E0_b)^+ cbar_b for every problem in one stacked solve: each system is
-    # padded to the longest tape with identity rows (zero right-hand side there)
-    mm = max(tape0.m)
-    Ms = np.zeros((B, mm, mm))
-    rhs = np.zeros((B, mm))
+    _, cbar = batch_tape_combine(tape0, probe=ybar)
+    # v_b = -(T_b - E0_b)^+ cbar_b for every problem in one launch (device solves)
+    vs = E.tridiag_pinv_solve_batch(tape0.alpha, tape0.beta, tape0.m, e0_d, cv, cbar.contiguous())
+    K = tape0.K
+    A0 = torch.zeros((B, K), dtype=torch.float64, device=dev)
+    B0 = torch.zeros((B, K + 1), dtype=torch.float64, device=dev)
     for b in range(B):
         m = tape0.m[b]
         cvec = cv[b, :m]
-        Ms[b, :m, :m] = (np.diag(a_h[b, :m] - e0[b]) + np.diag(b_h[b, 1:m], 1) + np.diag(b_h[b, 1:m], -1)
-                         + np.outer(cvec, cvec))
-        Ms[b, m:, m:] = np.eye(mm - m)
-        rhs[b, :m] = cbar[b, :m] - np.dot(cbar[b, :m], cvec) * cvec
-    vs = -np.linalg.solve(Ms, rhs[..., None])[..., 0]
-    A0 = np.zeros((B, tape0.K))
-    B0 = np.zeros((B, tape0.K + 1))
-    for b in range(B):
-        m = tape0.m[b]
-        cvec = cv[b, :m]
-        v = vs[b, :m] - np.dot(vs[b, :m], cvec) * cvec
-        A0[b, :m] = eb_h[b] * cvec ** 2 + v * cvec
+        v = vs[b, :m]
+        A0[b, :m] = e0bar[b] * cvec ** 2 + v * cvec
         if m > 1:
-            B0[b, 1:m] = 2.0 * eb_h[b] * cvec[:-1] * cvec[1:] + v[:-1] * cvec[1:] + v[1:] * cvec[:-1]
-    batch_tape_reverse(tape0, torch.as_tensor(A0).to(dev), torch.as_tensor(B0).to(dev), theta_bar,
-                       ext_coef=torch.as_tensor(cv).to(dev), ext_vec=ybar)
+            B0[b, 1:m] = 2.0 * e0bar[b] * cvec[:-1] * cvec[1:] + v[:-1] * cvec[1:] + v[1:] * cvec[:-1]
+    batch_tape_reverse(tape0, A0, B0, theta_bar, ext_coef=cv.contiguous(), ext_vec=ybar)
     return theta_bar
 
 

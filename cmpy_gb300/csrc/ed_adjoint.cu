@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "ed_adjoint.cuh"
+#include "ed_lzcheck.cuh"
 
 namespace ed {
 
@@ -389,7 +390,11 @@ ED_API ed_status ed_lanczos_tape(ed_plan p, const double* d_start, int max_steps
   double* V = (double*)(base + L.off_vec);
   double* part = (double*)(base + L.off_part);
   double* scal = (double*)(base + L.off_scal);
-  double* n2 = scal + K + (K + 1);           // start norm^2
+  // scalar region: abar[K], bbar[K+1], c[K+2], tridiagonal work 5(K+2), 16 scalars
+  double* cvec = scal + K + (K + 1);
+  double* twork = cvec + (K + 2);
+  double* n2 = twork + 5 * (K + 2);          // start norm^2
+  TriResult* tri = (TriResult*)(n2 + 2);
   TapeState* st = (TapeState*)(base + L.off_state);
   ED_CUDA(cudaMemsetAsync(st, 0, sizeof(TapeState), s));
   ED_CUDA(cudaMemsetAsync(d_alpha, 0, K * sizeof(double), s));
@@ -408,9 +413,13 @@ ED_API ed_status ed_lanczos_tape(ed_plan p, const double* d_start, int max_steps
   if (!std::isfinite(hn2)) return fail(ED_ERR_NONFINITE, "start vector is not finite");
   if (hn2 == 0.0) { *h_steps = 0; return ED_OK; }
   const int Km = (int)std::min<int64_t>(K, D);
-  int stop = 0, m_conv = 0;
-  std::vector<double> ha, hb, hc;
-  for (int k = 0; k < Km && !stop && !m_conv; ++k) {
+  // convergence tests on a side stream, on the device (ed_lzcheck.cuh); the host never waits
+  const bool checks = check_every > 0 && tol > 0.0;
+  SideChecks chk;
+  ED_TRY(chk.init(checks ? Km / check_every + 1 : 0));
+  int launched = 0;
+  for (int k = 0; k < Km; ++k) {
+    if (checks && chk.stopped()) break;
     double* q = qv(k);
     double* qp = k > 0 ? qv(k - 1) : nullptr;
     int nl = 4;
@@ -423,26 +432,15 @@ ED_API ed_status ed_lanczos_tape(ed_plan p, const double* d_start, int max_steps
     k_tp_update<<<gv, TP_NT, 0, s>>>(w, q, qp, D, d_alpha, d_beta, k, breakdown, part, st);
     k_tp_scale<<<gs, 256, 0, s>>>(w, qv(k + 1), D, d_beta + k + 1, stopf);
     ED_CHECK_LAUNCH_N("ed_lanczos_tape step", nl);
-    if (check_every > 0 && (k + 1) % check_every == 0 && k + 1 < Km) {
-      // synchronisation point: the breakdown flag, and the convergence test on the host
-      ED_CUDA(cudaMemcpyAsync(&stop, stopf, sizeof(int), cudaMemcpyDeviceToHost, s));
-      if (tol > 0.0) {
-        ha.resize(k + 1);
-        hb.resize(k + 2);
-        ED_CUDA(cudaMemcpyAsync(ha.data(), d_alpha, (k + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
-        ED_CUDA(cudaMemcpyAsync(hb.data(), d_beta, (k + 2) * sizeof(double), cudaMemcpyDeviceToHost, s));
-      }
-      ED_CUDA(cudaStreamSynchronize(s));
-      if (!stop && tol > 0.0) {
-        const double e = host_tridiag_lowest(ha.data(), hb.data(), k + 1, hc);
-        if (std::fabs(hb[k + 1] * hc[k]) <= tol * std::max(1.0, std::fabs(e))) m_conv = k + 1;
-      }
-    }
+    launched = k + 1;
+    if (checks && (k + 1) % check_every == 0 && k + 1 < Km)
+      ED_TRY(chk.launch(s, d_alpha, d_beta, k + 1, tol, &st->stop, &st->steps, tri, cvec, twork));
   }
+  ED_TRY(chk.join(s));
   TapeState hs;
   ED_CUDA(cudaMemcpyAsync(&hs, st, sizeof(TapeState), cudaMemcpyDeviceToHost, s));
   ED_CUDA(cudaStreamSynchronize(s));
-  *h_steps = hs.stop ? hs.steps : (m_conv ? m_conv : Km);
+  *h_steps = hs.stop ? hs.steps : launched;
   return ED_OK;
 }
 

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "ed_adjoint.cuh"
+#include "ed_lzcheck.cuh"
 
 namespace ed {
 
@@ -461,6 +462,7 @@ using namespace ed;
 namespace {
 
 struct BLayout {
+  size_t off_tri = 0;
   int nvec, gx, nsw;
   size_t off_vec, off_part, off_psw, off_scal, off_int, total;
 };
@@ -487,6 +489,8 @@ BLayout blayout(const ed_plan_s* p, int B, int K, int c) {
   L.off_scal = o; o = bt_align(o + (size_t)B * (2 * K + 2) * sizeof(double));
   // stop, steps, m [B]; tickets [2][B]
   L.off_int = o; o = bt_align(o + (size_t)5 * B * sizeof(int));
+  // per problem: eigenvector and work of the device convergence tests, [B][6 (K + 2)]
+  L.off_tri = o; o = bt_align(o + (size_t)B * 6 * (K + 2) * sizeof(double));
   L.total = o;
   return L;
 }
@@ -588,10 +592,17 @@ ED_API ed_status ed_batch_lanczos_tape(ed_plan p, int B, const double* d_theta, 
   k_bt_scale<<<gv, BT_NT, 0, s>>>(d_start, qv(0), D, d_beta, K + 1, bs.stop, 1, 0);
   ED_CHECK_LAUNCH("k_bt_scale");
   const int Km = (int)std::min<int64_t>(K, D);
-  std::vector<double> ha, hb, hc;
   std::vector<int> hsteps(B, 0);
+  // convergence tests of all live problems on a side stream, one block per problem, on the
+  // device (ed_lzcheck.cuh); the host never waits for them
+  const bool checks = check_every > 0 && tol > 0.0;
+  SideChecks chk;
+  ED_TRY(chk.init(checks ? Km / check_every + 1 : 0, B));
+  double* tvec = (double*)(base + L.off_tri);
+  const int ldw = K + 2;
   int k = 0;
   for (; k < Km && live > 0; ++k) {
+    if (checks && chk.stopped()) break;
     double* q = qv(k);
     double* qp = k > 0 ? qv(k - 1) : nullptr;
     int nl = 4;
@@ -604,45 +615,25 @@ ED_API ed_status ed_batch_lanczos_tape(ed_plan p, int B, const double* d_theta, 
     k_bt_update<<<gv, BT_NT, 0, s>>>(w, q, qp, D, d_alpha, d_beta, K, k, breakdown, part, bs);
     k_bt_scale<<<gv, BT_NT, 0, s>>>(w, qv(k + 1), D, d_beta + k + 1, K + 1, bs.stop, 1, k);
     ED_CHECK_LAUNCH_N("ed_batch_lanczos_tape step", nl);
-    if (check_every > 0 && (k + 1) % check_every == 0 && k + 1 < Km) {
-      // synchronisation point: breakdown flags, and the convergence tests on the host
+    if (checks && (k + 1) % check_every == 0 && k + 1 < Km) {
       const int kd = k + 1;
-      ED_CUDA(cudaMemcpyAsync(hstop.data(), bs.stop, B * sizeof(int), cudaMemcpyDeviceToHost, s));
-      if (tol > 0.0) {
-        ha.resize((size_t)B * K);
-        hb.resize((size_t)B * (K + 1));
-        ED_CUDA(cudaMemcpyAsync(ha.data(), d_alpha, (size_t)B * K * sizeof(double), cudaMemcpyDeviceToHost, s));
-        ED_CUDA(cudaMemcpyAsync(hb.data(), d_beta, (size_t)B * (K + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
-      }
-      ED_CUDA(cudaStreamSynchronize(s));
-      bool changed = false;
-      live = 0;
-      for (int b = 0; b < B; ++b) {
-        if (hstop[b]) continue;
-        if (tol > 0.0) {
-          const double* a = ha.data() + (size_t)b * K;
-          const double* bb = hb.data() + (size_t)b * (K + 1);
-          const double e = host_tridiag_lowest(a, bb, kd, hc);
-          if (std::fabs(bb[kd] * hc[kd - 1]) <= tol * std::max(1.0, std::fabs(e))) {
-            m_conv[b] = kd;
-            hstop[b] = 1;
-            changed = true;
-            continue;
-          }
-        }
-        ++live;
-      }
-      if (changed) ED_CUDA(cudaMemcpyAsync(bs.stop, hstop.data(), B * sizeof(int), cudaMemcpyHostToDevice, s));
+      ED_TRY(chk.launch(
+          s,
+          [&](cudaStream_t s2) {
+            k_tri_check_batch<<<B, TRI_NT, 0, s2>>>(d_alpha, d_beta, K, kd, tol, bs.stop, bs.steps, tvec,
+                                                     tvec + (size_t)B * ldw, ldw);
+          },
+          bs.stop));
     }
   }
+  ED_TRY(chk.join(s));
   ED_CUDA(cudaMemcpyAsync(hstop.data(), bs.stop, B * sizeof(int), cudaMemcpyDeviceToHost, s));
   ED_CUDA(cudaMemcpyAsync(hsteps.data(), bs.steps, B * sizeof(int), cudaMemcpyDeviceToHost, s));
   ED_CUDA(cudaStreamSynchronize(s));
   for (int b = 0; b < B; ++b) {
     if (hn2[b] == 0.0) h_steps[b] = 0;
-    else if (hstop[b] == 2) h_steps[b] = hsteps[b];
-    else if (m_conv[b]) h_steps[b] = m_conv[b];
-    else h_steps[b] = k;  // all steps run while the problem was live
+    else if (hstop[b]) h_steps[b] = hsteps[b];  // converged or invariant subspace
+    else h_steps[b] = k;                         // every launched step ran for it
   }
   return ED_OK;
 }

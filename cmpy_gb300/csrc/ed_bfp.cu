@@ -18,6 +18,7 @@
 #include <cmath>
 #include <vector>
 
+#include "ed_lzcheck.cuh"
 #include "ed_plan.cuh"
 #include "ed_sweep_tables.h"
 #include "ed_tridiag.cuh"
@@ -655,7 +656,6 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
   const int tid = threadIdx.x, nt = blockDim.x;
   const int64_t ngroups = (nu + MV3_R - 1) / MV3_R;
   const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
-  const unsigned row_bytes = (unsigned)(nd * 8);
 
   // stage group g from thread 0: bulk copies of its rows into `raw` and of its precomputed
   // padded up-lists and counts (rows u0, u0 + 1; row nu is an empty list) into list buffer s.
@@ -1076,6 +1076,28 @@ __global__ void k_bfp_ritz(const BfpVecs v, const int64_t* __restrict__ C, const
   }
 }
 
+// Ritz coefficients C_k = round(c_k / beta_k * 2^(e_k + SC)) of the final eigenvector c (one
+// block): one SC for all k with |C_k| < 2^62 - 10 bits of headroom for the sum over k
+__global__ void k_bfp_ritz_coef(const double* __restrict__ c, const double* __restrict__ beta,
+                                const int32_t* __restrict__ eR, const TriResult* tr, int64_t* C, int* SCp) {
+  __shared__ unsigned long long sm[BT / 32];
+  __shared__ int sc_s;
+  const int m = tr->m_final;
+  unsigned long long gb = 0;  // max |c_k / beta_k * 2^e_k| as bits (non-negative doubles order as integers)
+  for (int k = threadIdx.x; k < m; k += BT)
+    gb = max(gb, (unsigned long long)__double_as_longlong(fabs(ldexp(c[k] / beta[k], eR[k]))));
+  gb = block_max_u64<BT>(gb, sm);
+  if (threadIdx.x == 0) {
+    const double gm = __longlong_as_double((long long)gb);
+    int eg = 0;
+    frexp(gm > 0.0 ? gm : 1.0, &eg);
+    sc_s = 52 - eg;
+    *SCp = sc_s;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < m; k += BT) C[k] = llrint(ldexp(c[k] / beta[k], eR[k] + sc_s));
+}
+
 // ---- tables ---------------------------------------------------------------------------------------------
 
 static bool is_int_scaled(double v, int F, int64_t lim) {
@@ -1093,7 +1115,7 @@ static size_t sweep_smem_dn(int r) {
 }
 
 // Tables of the banded two-pass matvec (ed_sweep.cuh); leaves B.sw.on = 0 when the sector does
-// not suit it (odd num_dn: the 16-byte bulk row copies need even rows; a target with more than
+// not suit it (odd num_dn: the 16-byte row-piece copies of pass 1 need even rows; a target with more than
 // 15 hops; a band wider than the shared memory). CMPY_ED_SWEEP=0 disables it.
 static ed_status build_sweep(ed_plan_s* p, BfpTables& B, const std::vector<int32_t>& uoff,
                              const std::vector<int32_t>& uidx, const std::vector<double>& ucoef,
@@ -1109,8 +1131,9 @@ static ed_status build_sweep(ed_plan_s* p, BfpTables& B, const std::vector<int32
   if (nu < 1 || nd < 2 || nd % 2) return ED_OK;
   SweepSide su, sd;
   if (!sweep_order(nu, uoff, uidx, ucoef, &su) || !sweep_order(nd, doff, didx, dcoef, &sd)) return ED_OK;
-  // rings: as many chunks as two CTAs per SM allow (extra chunks are prefetch room), else as
-  // many as one CTA per SM allows
+  // rings: as many chunks as one CTA per SM allows: the chunks beyond the band window are the
+  // prefetch depth, and with two CTAs per SM the window left ~1-2 chunks of it (the passes
+  // then waited on every chunk); CMPY_ED_SWEEP_CTAS=2 selects the two-per-SM rings
   int per_sm = 0;
   ED_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, p->device));
   const size_t two = (size_t)per_sm / 2 - 2048, one = (size_t)p->ctx->smem_optin - 1024;
@@ -1118,7 +1141,11 @@ static ed_status build_sweep(ed_plan_s* p, BfpTables& B, const std::vector<int32
     int r2 = 0, r1 = 0;
     while (smem(r2 + 1) <= two) ++r2;
     while (smem(r1 + 1) <= one) ++r1;
-    const int r = need <= r2 ? r2 : (need <= r1 ? r1 : 0);
+    static const int per = [] {
+      const char* e = getenv("CMPY_ED_SWEEP_CTAS");
+      return e ? atoi(e) : 1;
+    }();
+    const int r = (per == 2 && need <= r2) ? r2 : (need <= r1 ? r1 : 0);
     if (r == 0) return 0;
     return (int)std::min<int64_t>(std::max<int64_t>(need, std::min<int64_t>(r, nchunks)), 32767 / SW_CH);
   };
@@ -1402,7 +1429,10 @@ void free_bfp(ed_plan_s* p) {
 }
 
 // first-wait limit of the bulk-copy matvecs (polls); 0 selects MV3_WAIT_LIMIT
-static long wait_limit(const ed_plan_s* p) { return p->bfp.wait_limit > 0 ? p->bfp.wait_limit : MV3_WAIT_LIMIT; }
+// (-1: no test at all, the first wait gives up at once)
+static long wait_limit(const ed_plan_s* p) {
+  return p->bfp.wait_limit > 0 ? p->bfp.wait_limit : (p->bfp.wait_limit < 0 ? 0 : MV3_WAIT_LIMIT);
+}
 
 static BfpHubArgs bfp_args(const ed_plan_s* p) {
   const BfpTables& B = p->bfp;
@@ -1467,8 +1497,12 @@ static int matvec_variant(const ed_plan_s* p) {
   if (forced == 2) return v2_ok ? 2 : 1;
   if (forced == 3 && v3_ok) return 3;
   if (forced == 4 && v4_ok) return 4;  // measured slower than 3 on GB300 (kept for comparison)
-  if (v5_ok && (forced == 0 || forced == 5)) return 5;
+  // the sweep (5) only when asked for, or where the single-pass kernel does not fit: on the
+  // 14-site sectors it measured 0.75 ms per H*v against 0.19 ms for 3 (its pass walks one
+  // stripe per CTA through the band and waits on every chunk)
+  if (v5_ok && forced == 5) return 5;
   if (v3_ok) return 3;
+  if (v5_ok) return 5;
   return v2_ok ? 2 : 1;
 }
 
@@ -1623,7 +1657,8 @@ static ed_status launch_bfp_matvec(const ed_plan_s* p, const int64_t* X, int64_t
 
 // ---- the BFP Lanczos driver ----------------------------------------------------------------------
 struct BfpLayout {
-  size_t off_R, off_W, off_eR, off_maxR, off_part, off_partmax, off_c, off_C, off_work, off_state, off_misc, total;
+  size_t off_R, off_W, off_eR, off_maxR, off_part, off_partmax, off_c, off_C, off_work, off_state, off_misc, off_tri,
+      total;
   int nslots, nparts;
 };
 
@@ -1646,6 +1681,7 @@ static BfpLayout bfp_layout(const ed_plan_s* p, int K, bool store) {
   L.off_work = o; o = al256(o + (size_t)5 * (K + 2) * 8);
   L.off_state = o; o = al256(o + sizeof(BfpState));
   L.off_misc = o; o = al256(o + 64);
+  L.off_tri = o; o = al256(o + sizeof(TriResult));
   L.total = o;
   return L;
 }
@@ -1661,6 +1697,7 @@ struct BfpRun {
   int64_t* C;
   BfpState* st;
   int* misc;
+  TriResult* tri;
 };
 
 static BfpRun bfp_bind(const ed_plan_s* p, void* work, int K, bool store) {
@@ -1680,6 +1717,7 @@ static BfpRun bfp_bind(const ed_plan_s* p, void* work, int K, bool store) {
   r.work = (double*)(b + r.L.off_work);
   r.st = (BfpState*)(b + r.L.off_state);
   r.misc = (int*)(b + r.L.off_misc);
+  r.tri = (TriResult*)(b + r.L.off_tri);
   return r;
 }
 
@@ -1770,11 +1808,14 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
     ev.resize(2 * (size_t)Km);
     for (auto& e : ev) ED_CUDA(cudaEventCreate(&e));
   }
-  // convergence tests and the final eigenpair of T run on the host (a chain of dependent FP64
-  // operations: tens of µs on a host core, milliseconds in one block of this GPU)
-  std::vector<double> ha, hb, hc;
-  int m_conv = 0, launched = 0;
-  for (int k = 0; k < Km && !m_conv; ++k) {
+  // convergence tests on a side stream and the final eigenpair, on the device (ed_lzcheck.cuh)
+  const bool checks = prm->check_every > 0 && prm->tol > 0.0;
+  SideChecks chk;
+  ED_TRY(chk.init(checks ? Km / prm->check_every + 1 : 0));
+  ED_CUDA(cudaMemsetAsync(r.tri, 0, sizeof(TriResult), s));
+  int launched = 0;
+  for (int k = 0; k < Km; ++k) {
+    if (checks && chk.stopped()) break;
     if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k], s));
     const BfpFuse fz = bfp_fuse(p, r, k, alpha, beta);
     bool fused = false;
@@ -1786,55 +1827,30 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
     ED_TRY(launch_update(p, r, k, alpha, beta, s));
     ED_CHECK_LAUNCH_N("bfp lanczos step", fused ? 1 : 2);
     launched = k + 1;
-    if (prm->check_every > 0 && prm->tol > 0.0 && ((k + 1) % prm->check_every == 0) && k + 1 < Km) {
-      int hstop = 0;
-      ha.resize(k + 1);
-      hb.resize(k + 2);
-      ED_CUDA(cudaMemcpyAsync(&hstop, &r.st->stop, sizeof(int), cudaMemcpyDeviceToHost, s));
-      ED_CUDA(cudaMemcpyAsync(ha.data(), alpha, (k + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
-      ED_CUDA(cudaMemcpyAsync(hb.data(), beta, (k + 2) * sizeof(double), cudaMemcpyDeviceToHost, s));
-      ED_CUDA(cudaStreamSynchronize(s));
-      if (hstop) break;  // invariant subspace or a failed wait: the device state says which
-      const double e = host_tridiag_lowest(ha.data(), hb.data(), k + 1, hc);
-      if (std::fabs(hb[k + 1] * hc[k]) <= prm->tol * std::max(1.0, std::fabs(e))) m_conv = k + 1;
-    }
+    if (checks && ((k + 1) % prm->check_every == 0) && k + 1 < Km)
+      ED_TRY(chk.launch(s, alpha, beta, k + 1, prm->tol, &r.st->stop, &r.st->steps, r.tri, r.c, r.work));
   }
-  BfpState hs;
-  ED_CUDA(cudaMemcpyAsync(&hs, r.st, sizeof(BfpState), cudaMemcpyDeviceToHost, s));
-  ED_CUDA(cudaStreamSynchronize(s));
-  if (hs.status == DEV_TIMEOUT) return fail(ED_ERR_TIMEOUT, "fixed-point matvec: a bounded wait for a row copy ran out");
-  const int m = hs.stop ? hs.steps : (m_conv ? m_conv : launched);
-  ha.resize(m);
-  hb.resize(m + 1);
-  ED_CUDA(cudaMemcpyAsync(ha.data(), alpha, m * sizeof(double), cudaMemcpyDeviceToHost, s));
-  ED_CUDA(cudaMemcpyAsync(hb.data(), beta, (m + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
-  std::vector<int32_t> he(m);
-  if (evec) ED_CUDA(cudaMemcpyAsync(he.data(), r.v.eR, m * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-  ED_CUDA(cudaStreamSynchronize(s));
-  const double e0 = host_tridiag_lowest(ha.data(), hb.data(), m, hc);
+  ED_TRY(chk.join(s));
+  k_tri_final<<<1, TRI_NT, 0, s>>>(alpha, beta, launched, &r.st->stop, &r.st->steps, r.tri, r.c, r.work);
+  ED_CHECK_LAUNCH("k_tri_final");
   if (evec) {
-    // Ritz coefficients C_k = round(c_k / beta_k * 2^(e_k + SC)), one SC for all k with
-    // |C_k| < 2^62 - 10 bits of headroom for the sum over k
-    double gm = 0.0;
-    for (int k = 0; k < m; ++k) gm = std::max(gm, std::fabs(std::ldexp(hc[k] / hb[k], he[k])));
-    int eg = 0;
-    std::frexp(gm > 0.0 ? gm : 1.0, &eg);
-    const int SC = 52 - eg;
-    std::vector<int64_t> hC(m);
-    for (int k = 0; k < m; ++k) hC[k] = std::llrint(std::ldexp(hc[k] / hb[k], he[k] + SC));
-    ED_CUDA(cudaMemcpyAsync(r.C, hC.data(), m * sizeof(int64_t), cudaMemcpyHostToDevice, s));
-    ED_CUDA(cudaMemcpyAsync(r.misc, &SC, sizeof(int), cudaMemcpyHostToDevice, s));
-    ED_CUDA(cudaMemcpyAsync(&r.st->steps, &m, sizeof(int), cudaMemcpyHostToDevice, s));
+    k_bfp_ritz_coef<<<1, BT, 0, s>>>(r.c, beta, r.v.eR, r.tri, r.C, r.misc);
     k_bfp_ritz<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(
         r.v, r.C, r.misc, r.st, evec, renum ? p->bfp.sw.perm_up : nullptr, renum ? p->bfp.sw.perm_dn : nullptr,
         p->num_dn);
-    ED_CHECK_LAUNCH("k_bfp_ritz");
-    ED_CUDA(cudaStreamSynchronize(s));  // the host arrays above are sources of the copies
+    ED_CHECK_LAUNCH_N("k_bfp_ritz", 2);
   }
-  res->energy = e0;
-  res->residual = std::fabs(hb[m] * hc[m - 1]);
+  BfpState hs;
+  TriResult ht;
+  ED_CUDA(cudaMemcpyAsync(&hs, r.st, sizeof(BfpState), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(&ht, r.tri, sizeof(TriResult), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  if (hs.status == DEV_TIMEOUT) return fail(ED_ERR_TIMEOUT, "fixed-point matvec: a bounded wait for a row copy ran out");
+  const int m = ht.m_final;
+  res->energy = ht.energy;
+  res->residual = ht.residual;
   res->steps = m;
-  res->converged = hs.stop ? hs.stop : (m_conv ? 1 : 0);
+  res->converged = hs.stop;
   res->status = hs.status;
   res->matvec_ms = 0.0;
   res->matvecs = 0;
@@ -1965,7 +1981,7 @@ ED_API ed_status ed_matvec_fixed(ed_plan p, const int64_t* d_xm, int32_t ex, int
 
 ED_API ed_status ed_plan_set_wait_limit(ed_plan p, int64_t polls) {
   ED_TRY(check_plan(p));
-  if (polls < 0) return fail(ED_ERR_INVALID_ARG, "polls must be >= 0");
+  if (polls < -1) return fail(ED_ERR_INVALID_ARG, "polls must be >= -1");
   p->bfp.wait_limit = (long)polls;
   return ED_OK;
 }

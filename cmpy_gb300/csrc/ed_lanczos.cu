@@ -1,9 +1,9 @@
 // Device Lanczos: the ground state that cmpy obtains from ARPACK eigsh(k=1, which="SA")
 // (cmpy/exactdiag.py:24-43) and the Lanczos coefficients of cmpy/exactdiag.py:324-375,
 // run on the GPU. The recurrence's scalars (alpha, beta, norms, flags) stay in device memory
-// and the host enqueues the steps without waiting; it reads the scalars only at the
-// convergence tests and at the end, where it solves the small tridiagonal eigenproblem (a
-// chain of dependent FP64 operations, which a host core runs far faster than one GPU block).
+// and the host enqueues the steps without waiting; the convergence tests and the final
+// tridiagonal eigenpair also run on the device (ed_lzcheck.cuh), so the host waits once, at
+// the end.
 //
 // Reductions are deterministic: each block writes a partial, the last block to arrive
 // (atomic ticket, no waiting) sums the partials in block order.
@@ -11,6 +11,7 @@
 #include <cmath>
 #include <vector>
 
+#include "ed_lzcheck.cuh"
 #include "ed_plan.cuh"
 #include "ed_tridiag.cuh"
 
@@ -302,6 +303,28 @@ __global__ void __launch_bounds__(RA_NT, 6) k_multiaxpy(const double* __restrict
   }
 }
 
+// B tridiagonals, one block each: problem b has alpha[b*lda ..], beta[b*ldb ..], size m[b]
+__global__ void k_tridiag_batch(const double* alpha, int lda, const double* beta, int ldb, const int* m, double* value,
+                                double* vec, int ldv, double* work) {
+  const int b = blockIdx.x;
+  if (m[b] < 1) {  // an empty run (zero start vector)
+    if (threadIdx.x == 0) value[b] = 0.0;
+    return;
+  }
+  const double e = tridiag_lowest_block<512>(alpha + (size_t)b * lda, beta + (size_t)b * ldb, m[b],
+                                             vec ? vec + (size_t)b * ldv : nullptr, work + (size_t)b * 5 * ldv);
+  if (threadIdx.x == 0) value[b] = e;
+}
+
+__global__ void k_tridiag_pinv_batch(const double* alpha, int lda, const double* beta, int ldb, const int* m,
+                                     const double* e0, const double* c, int ldc, const double* rhs, double* out,
+                                     int ldr, double* work) {
+  const int b = blockIdx.x;
+  if (m[b] < 1) return;
+  tridiag_pinv_solve(alpha + (size_t)b * lda, beta + (size_t)b * ldb, m[b], e0[b], c + (size_t)b * ldc,
+                     rhs + (size_t)b * ldr, out + (size_t)b * ldr, work + (size_t)b * 5 * ldr);
+}
+
 __global__ void k_tridiag(const double* alpha, const double* beta, int m, double* value, double* vec, double* work) {
   const double e = tridiag_lowest_block<512>(alpha, beta, m, vec, work);
   if (threadIdx.x == 0) *value = e;
@@ -321,7 +344,7 @@ __global__ void k_ritz(const double* __restrict__ Q, int64_t ldq, const double* 
 // ---- workspace layout ----------------------------------------------------------------------
 struct LzLayout {
   int64_t nvec;      // vectors in the basis store
-  size_t off_basis, off_w, off_partial, off_h, off_c, off_work, off_state, off_scalars, total;
+  size_t off_basis, off_w, off_partial, off_h, off_c, off_work, off_state, off_scalars, off_tri, total;
   int nparts;
 };
 
@@ -340,6 +363,7 @@ static LzLayout lz_layout(int64_t D, int K, bool store, int nparts) {
   L.off_work = o; o = align256(o + (size_t)5 * (K + 2) * sizeof(double));
   L.off_scalars = o; o = align256(o + 8 * sizeof(double));
   L.off_state = o; o = align256(o + sizeof(LzState));
+  L.off_tri = o; o = align256(o + sizeof(TriResult));
   L.total = o;
   return L;
 }
@@ -443,7 +467,10 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
   double* c = (double*)(base + L.off_c);
   double* scal = (double*)(base + L.off_scalars);
   LzState* st = (LzState*)(base + L.off_state);
+  double* twork = (double*)(base + L.off_work);
+  TriResult* tri = (TriResult*)(base + L.off_tri);
   ED_CUDA(cudaMemsetAsync(st, 0, sizeof(LzState), s));
+  ED_CUDA(cudaMemsetAsync(tri, 0, sizeof(TriResult), s));
   ED_CUDA(cudaMemsetAsync(d_alpha, 0, K * sizeof(double), s));
   ED_CUDA(cudaMemsetAsync(d_beta, 0, (K + 1) * sizeof(double), s));
   const int gv = nparts;
@@ -482,11 +509,13 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
   // the Krylov dimension cannot exceed D; without reorthogonalisation rounding would
   // otherwise keep beta alive past it
   const int Km = (int)std::min<int64_t>(K, D);
-  // convergence tests and the final eigenpair of T run on the host (a chain of dependent FP64
-  // operations: tens of µs on a host core, milliseconds in one block of this GPU)
-  std::vector<double> ha, hb, hc;
-  int m_conv = 0, launched = 0;
-  for (int k = 0; k < Km && !m_conv; ++k) {
+  // convergence tests on a side stream and the final eigenpair, on the device (ed_lzcheck.cuh)
+  const bool checks = prm->check_every > 0 && prm->tol > 0.0;
+  SideChecks chk;
+  ED_TRY(chk.init(checks ? Km / prm->check_every + 1 : 0));
+  int launched = 0;
+  for (int k = 0; k < Km; ++k) {
+    if (checks && chk.stopped()) break;
     double* q = qv(k);
     double* qp = k > 0 ? qv(k - 1) : nullptr;
     if (prm->profile) ED_CUDA(cudaEventRecord(ev[2 * k], s));
@@ -507,42 +536,28 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
     k_scale<<<gs, 256, 0, s>>>(w, qv(k + 1), D, d_beta + k + 1, stopf);
     ED_CHECK_LAUNCH_N("lanczos step", nl);
     launched = k + 1;
-    if (prm->check_every > 0 && prm->tol > 0.0 && ((k + 1) % prm->check_every == 0) && k + 1 < Km) {
-      int hstop = 0;
-      ha.resize(k + 1);
-      hb.resize(k + 2);
-      ED_CUDA(cudaMemcpyAsync(&hstop, stopf, sizeof(int), cudaMemcpyDeviceToHost, s));
-      ED_CUDA(cudaMemcpyAsync(ha.data(), d_alpha, (k + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
-      ED_CUDA(cudaMemcpyAsync(hb.data(), d_beta, (k + 2) * sizeof(double), cudaMemcpyDeviceToHost, s));
-      ED_CUDA(cudaStreamSynchronize(s));
-      if (hstop) break;  // invariant subspace
-      const double e = host_tridiag_lowest(ha.data(), hb.data(), k + 1, hc);
-      if (std::fabs(hb[k + 1] * hc[k]) <= prm->tol * std::max(1.0, std::fabs(e))) m_conv = k + 1;
-    }
+    if (checks && ((k + 1) % prm->check_every == 0) && k + 1 < Km)
+      ED_TRY(chk.launch(s, d_alpha, d_beta, k + 1, prm->tol, &st->stop, &st->steps, tri, c, twork));
   }
-  LzState hs;
-  ED_CUDA(cudaMemcpyAsync(&hs, st, sizeof(LzState), cudaMemcpyDeviceToHost, s));
-  ED_CUDA(cudaStreamSynchronize(s));
-  const int m = hs.stop ? hs.steps : (m_conv ? m_conv : launched);
-  ha.resize(m);
-  hb.resize(m + 1);
-  ED_CUDA(cudaMemcpyAsync(ha.data(), d_alpha, m * sizeof(double), cudaMemcpyDeviceToHost, s));
-  ED_CUDA(cudaMemcpyAsync(hb.data(), d_beta, (m + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
-  ED_CUDA(cudaStreamSynchronize(s));
-  const double e0 = host_tridiag_lowest(ha.data(), hb.data(), m, hc);
+  ED_TRY(chk.join(s));
+  k_tri_final<<<1, TRI_NT, 0, s>>>(d_alpha, d_beta, launched, &st->stop, &st->steps, tri, c, twork);
+  ED_CHECK_LAUNCH("k_tri_final");
   if (prm->want_vector) {
-    ED_CUDA(cudaMemcpyAsync(c, hc.data(), m * sizeof(double), cudaMemcpyHostToDevice, s));
-    ED_CUDA(cudaMemcpyAsync(&st->steps, &m, sizeof(int), cudaMemcpyHostToDevice, s));
     k_ritz<<<gs, 256, 0, s>>>(Q, D, c, st, d_evec, D);
     k_dot<<<gv, LZ_NT, 0, s>>>(d_evec, d_evec, D, part, st, 0, scal, scal + 1, nullptr);
     k_scale<<<gs, 256, 0, s>>>(d_evec, d_evec, D, scal + 1, nullptr);
     ED_CHECK_LAUNCH_N("lanczos ritz", 3);
-    ED_CUDA(cudaStreamSynchronize(s));  // the host arrays above are sources of the copies
   }
-  res->energy = e0;
-  res->residual = std::fabs(hb[m] * hc[m - 1]);
+  LzState hs;
+  TriResult ht;
+  ED_CUDA(cudaMemcpyAsync(&hs, st, sizeof(LzState), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(&ht, tri, sizeof(TriResult), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  const int m = ht.m_final;
+  res->energy = ht.energy;
+  res->residual = ht.residual;
   res->steps = m;
-  res->converged = hs.stop ? hs.stop : (m_conv ? 1 : 0);
+  res->converged = hs.stop;
   res->status = hs.status;
   res->matvec_ms = 0.0;
   res->matvecs = 0;
@@ -611,6 +626,40 @@ ED_API ed_status ed_lanczos_coeffs(ed_plan p, int K, const double* d_start, void
   ED_CUDA(cudaStreamSynchronize(s));
   *h_steps = hs.stop ? hs.steps : Km;
   *h_norm = std::sqrt(n2);
+  return ED_OK;
+}
+
+ED_API ed_status ed_tridiag_lowest_batch(const double* d_alpha, int lda, const double* d_beta, int ldb,
+                                         const int* d_m, int B, int max_m, double* d_values, double* d_vecs, int ldv,
+                                         ed_stream_t stream) {
+  if (B < 0 || max_m < 1 || max_m > 4096 || lda < max_m || ldb < max_m + 1 || ldv < max_m)
+    return fail(ED_ERR_INVALID_ARG, "bad batch shape (1 <= m <= 4096, lda >= m, ldb >= m + 1, ldv >= m)");
+  if (B == 0) return ED_OK;
+  if (!d_alpha || !d_beta || !d_m || !d_values || !d_vecs) return fail(ED_ERR_INVALID_ARG, "null argument");
+  cudaStream_t s = as_stream(stream);
+  double* work = nullptr;
+  ED_CUDA(cudaMallocAsync(&work, 5 * (size_t)B * ldv * sizeof(double), s));
+  k_tridiag_batch<<<B, LZ_NT, 0, s>>>(d_alpha, lda, d_beta, ldb, d_m, d_values, d_vecs, ldv, work);
+  ED_CHECK_LAUNCH("k_tridiag_batch");
+  ED_CUDA(cudaFreeAsync(work, s));
+  return ED_OK;
+}
+
+ED_API ed_status ed_tridiag_pinv_solve_batch(const double* d_alpha, int lda, const double* d_beta, int ldb,
+                                             const int* d_m, int B, int max_m, const double* d_e0, const double* d_c,
+                                             int ldc, const double* d_rhs, double* d_out, int ldr,
+                                             ed_stream_t stream) {
+  if (B < 0 || max_m < 1 || max_m > 4096 || lda < max_m || ldb < max_m + 1 || ldc < max_m || ldr < max_m)
+    return fail(ED_ERR_INVALID_ARG, "bad batch shape (1 <= m <= 4096, leading dimensions >= m)");
+  if (B == 0) return ED_OK;
+  if (!d_alpha || !d_beta || !d_m || !d_e0 || !d_c || !d_rhs || !d_out) return fail(ED_ERR_INVALID_ARG, "null argument");
+  if (d_rhs == d_out) return fail(ED_ERR_INVALID_ARG, "d_rhs and d_out must not alias");
+  cudaStream_t s = as_stream(stream);
+  double* work = nullptr;
+  ED_CUDA(cudaMallocAsync(&work, 5 * (size_t)B * ldr * sizeof(double), s));
+  k_tridiag_pinv_batch<<<B, 32, 0, s>>>(d_alpha, lda, d_beta, ldb, d_m, d_e0, d_c, ldc, d_rhs, d_out, ldr, work);
+  ED_CHECK_LAUNCH("k_tridiag_pinv_batch");
+  ED_CUDA(cudaFreeAsync(work, s));
   return ED_OK;
 }
 

@@ -14,11 +14,11 @@
 //   gathered into it and the Ritz vector scattered back. alpha and beta do not change: every
 //   dot product is an exact integer sum per element.
 // * Pass 1 (k_sweep_up): one CTA per 16-column stripe of X walks down the rows in blocks of
-//   32. A ring of row chunks (32 rows x 16 columns = 4 KB, one 128-byte bulk copy per row,
-//   completion on the chunk's mbarrier) holds the band around the current block; each chunk
-//   is copied once. A half-warp forms one target row's 16 sums S = A X from its hop list
-//   (entries are precomputed ring offsets), lane = column, so a gather reads one contiguous
-//   128-byte ring row (one shared-memory wavefront). Output S goes to the W buffer.
+//   32. A ring of row chunks (32 rows x 16 columns = 4 KB as 256 16-byte async copies, each
+//   thread arriving on the chunk's mbarrier once its copy has landed) holds the band around
+//   the current block; each chunk is copied once. A half-warp forms one target row's 16 sums
+//   S = A X from its hop list (entries are precomputed ring offsets), lane = column, so a
+//   gather reads one contiguous 128-byte ring row (one shared-memory wavefront). Output S goes to the W buffer.
 // * Pass 2 (k_sweep_dn): one CTA per 16-row stripe walks along the columns in blocks of 32. A
 //   ring of column chunks (16 rows x 32 columns, 8-byte async copies) is laid out with a row
 //   stride of (ring columns + 1) elements, so the 16 rows of one column sit in 16 different
@@ -38,6 +38,15 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src, uint64_t p
   asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src), "l"(pol)
                : "memory");
 }
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, uint64_t pol) {
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "l"(pol)
+               : "memory");
+}
+// after a wait gave up: let copies that may still be in flight land before the CTA leaves
+// (about 0.1 ms; a copy takes microseconds)
+__device__ __forceinline__ void sweep_settle() {
+  for (int i = 0; i < 3000; ++i) __nanosleep(32);
+}
 // arrive on `bar` once this thread's earlier cp.async copies have landed (no pending-count
 // increment: the barrier is initialised with one arrival per thread)
 __device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
@@ -45,13 +54,32 @@ __device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+static_assert(SW_NT >= SW_CH * SW_W / 2, "pass 1 copies a chunk as 16-byte pieces, one per thread");
+static_assert(SW_NT == SW_CH * SW_W, "pass 2 copies a chunk as 8-byte elements, one per thread");
+
 // L2 policy of the sweep's memory streams, by selector bit (1 = evict_last, 0 = evict_first)
 __device__ __forceinline__ uint64_t sweep_policy(int sel, int bit) {
   return ((sel >> bit) & 1) ? policy_evict_last() : policy_evict_first();
 }
 
-// 64-bit value of uint16 entry e (compile-time e) of a list held in eight 32-bit words
-#define SW_ENTRY(w, e) (((e) & 1) ? ((w)[(e) >> 1] >> 16) : ((w)[(e) >> 1] & 0xffffu))
+// sum of one target's hop partners from a ring: base points at the target's column (pass 1:
+// ring row r at base[r * STRIDE]) or row (pass 2: ring column r at base[r]); le is the hop list
+// in shared memory (entries with positive sign first, entry 15 = count | positive count << 8)
+template <int STRIDE>
+__device__ __forceinline__ int64_t sweep_hops(const int64_t* __restrict__ base, const uint16_t* le) {
+  const uint32_t cw = le[SW_LST - 1];
+  const int cnt = (int)(cw & 0xffu), npos = (int)(cw >> 8);
+  int64_t h0 = 0, h1 = 0, hn = 0;
+  int e = 0;
+  for (; e + 4 <= npos; e += 4) {  // four independent gathers in flight
+    const uint2 pr = *(const uint2*)(le + e);
+    h0 += base[(pr.x & 0xffffu) * STRIDE] + base[(pr.x >> 16) * STRIDE];
+    h1 += base[(pr.y & 0xffffu) * STRIDE] + base[(pr.y >> 16) * STRIDE];
+  }
+  for (; e < npos; ++e) h0 += base[(uint32_t)le[e] * STRIDE];
+  for (; e < cnt; ++e) hn += base[(uint32_t)le[e] * STRIDE];
+  return (h0 + h1) - hn;
+}
 
 struct SweepArgs {
   int64_t nu, nd;
@@ -77,6 +105,23 @@ __device__ __forceinline__ void sweep_stage_lists(const uint16_t* lst, int64_t n
   bulk_g2s(lring + (size_t)slot * SW_CH * SW_LST, lst + t0 * SW_LST, bytes, &lbar[slot], policy_evict_last());
 }
 
+// after a wait gave up (thread 0, every thread past cp.async.wait_all): the chunk arrivals
+// those copies trigger and the staged list copies reach their barriers (bounded, the first
+// wait that runs out ends the waiting), then a short pause for anything still in flight
+__device__ __forceinline__ void sweep_drain(uint64_t* bar, uint64_t* lbar, int ring, int64_t ready, int64_t next,
+                                            int slot_w, unsigned par_w, int lwaited, int lstaged) {
+  bool ok = true;
+  for (; ok && ready < next - 1; ++ready) {
+    ok = mbar_wait_bounded(&bar[slot_w], par_w);
+    if (++slot_w == ring) {
+      slot_w = 0;
+      par_w ^= 1u;
+    }
+  }
+  for (int b = lwaited; ok && b < lstaged; ++b) ok = mbar_wait_bounded(&lbar[b % SW_LR], (unsigned)(b / SW_LR) & 1u);
+  sweep_settle();
+}
+
 // ---- pass 1: S = A X, column stripes -----------------------------------------------------------
 __global__ void __launch_bounds__(SW_NT, 2)
     k_sweep_up(SweepArgs a, const int64_t* __restrict__ X, int64_t* __restrict__ S, BfpState* st, int* status) {
@@ -90,17 +135,19 @@ __global__ void __launch_bounds__(SW_NT, 2)
   const int64_t c0 = (int64_t)blockIdx.x * SW_W;
   const int ncols = (int)min((int64_t)SW_W, a.nd - c0);
   const int64_t nchunks = (a.nu + SW_CH - 1) / SW_CH;
-  for (int i = tid; i < a.ring + SW_LR; i += SW_NT) mbar_init(&bar[i], 1);
   int lstaged = 0;   // list blocks staged (thread 0)
   int lwaited = 0;   // list blocks whose copy this thread has seen land
   if (tid == 0) {
+    // one thread initialises every barrier: its fence makes exactly those inits visible to
+    // the bulk copies (async proxy) that complete on them
+    for (int i = 0; i < a.ring; ++i) mbar_init(&bar[i], SW_NT);  // chunk barriers: one arrival per thread
+    for (int i = 0; i < SW_LR; ++i) mbar_init(&lbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     for (; lstaged < SW_LR && lstaged < a.nblk; ++lstaged) sweep_stage_lists(a.lst, a.nu, lstaged, lring, lbar, lstaged);
   }
   __syncthreads();
   const uint64_t pol_x = sweep_policy(a.pol, 0), pol_s = sweep_policy(a.pol, 1);
-  const unsigned row_bytes = (unsigned)ncols * 8u;
-  int64_t next = 0;          // next chunk to issue (warp 0)
+  int64_t next = 0;          // next chunk to issue
   int slot_i = 0;            // its ring slot
   int64_t ready = -1;        // chunks <= ready have landed (every thread waited for them)
   int slot_w = 0;
@@ -112,19 +159,18 @@ __global__ void __launch_bounds__(SW_NT, 2)
     const int2 w = w_next;
     if (j + 1 < a.nblk) w_next = __ldg(&a.win[j + 1]);  // one block ahead
     const int ls = j % SW_LR;
-    if (warp == 0) {
+    {
       // refill: chunks up to (first chunk still needed) + ring - 1; their slots were last read
-      // in blocks that every warp has finished (barrier at the end of the previous block)
+      // in blocks that every thread has finished (barrier at the end of the previous block).
+      // A chunk is 32 rows x 16 columns: threads 0..255 copy 16 bytes each, then every thread
+      // arrives on the chunk's barrier once its own copies have landed.
       const int64_t lim = min(nchunks - 1, (int64_t)w.x + a.ring - 1);
-      if (next <= lim) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      const int crow = tid >> 3, cpart = tid & 7;
       for (; next <= lim; ++next) {
-        const int64_t r0 = next * SW_CH;
-        const int nr = (int)min((int64_t)SW_CH, a.nu - r0);
-        if (lane == 0) mbar_expect_tx(&bar[slot_i], row_bytes * (unsigned)nr);
-        __syncwarp();
-        if (lane < nr)
-          bulk_g2s(ring + ((size_t)slot_i * SW_CH + lane) * SW_W, X + (r0 + lane) * a.nd + c0, row_bytes, &bar[slot_i],
-                   pol_x);
+        const int64_t r = next * SW_CH + crow;
+        if (tid < SW_CH * 8 && r < a.nu && 2 * cpart < ncols)
+          cp_async16(ring + ((size_t)slot_i * SW_CH + crow) * SW_W + 2 * cpart, X + r * a.nd + c0 + 2 * cpart, pol_x);
+        cp_async_arrive(&bar[slot_i]);
         if (++slot_i == a.ring) slot_i = 0;
       }
     }
@@ -145,26 +191,13 @@ __global__ void __launch_bounds__(SW_NT, 2)
       bad = true;
       break;
     }
-    const uint16_t* lb = lring + (size_t)ls * SW_CH * SW_LST;
-#pragma unroll
-    for (int q = 0; q < SW_CH / 16; ++q) {
-      const int ul = 16 * q + 2 * warp + half;
+    {
+      // half-warp = one target row of the block, lane = column of the stripe
+      const int ul = 2 * warp + half;
       const int64_t u = (int64_t)j * SW_CH + ul;
       if (u < a.nu) {
-        const uint4* lp = (const uint4*)(lb + ul * SW_LST);
-        const uint4 L0 = lp[0], L1 = lp[1];
-        const uint32_t wd[8] = {L0.x, L0.y, L0.z, L0.w, L1.x, L1.y, L1.z, L1.w};
-        const int cnt = (int)(wd[7] >> 16);
-        int64_t hp = 0, hn = 0;
-#pragma unroll
-        for (int e = 0; e < SW_LST - 1; ++e) {
-          if (e < cnt) {
-            const uint32_t en = SW_ENTRY(wd, e);
-            const int64_t v = ring[(size_t)(en & 0x7fffu) * SW_W + col];
-            if (en & 0x8000u) hn += v; else hp += v;
-          }
-        }
-        if (col < ncols) st_stream(S + u * a.nd + c0 + col, hp - hn, pol_s);
+        const int64_t hsum = sweep_hops<SW_W>(ring + col, lring + ((size_t)ls * SW_CH + ul) * SW_LST);
+        if (col < ncols) st_stream(S + u * a.nd + c0 + col, hsum, pol_s);
       }
     }
     __syncthreads();
@@ -177,23 +210,17 @@ __global__ void __launch_bounds__(SW_NT, 2)
   }
   if (bad) {
     // a wait ran out: record it, let every issued copy land (bounded), leave
+    cp_async_wait_all();
+    __syncthreads();
     if (tid == 0) {
       record_status(status, DEV_TIMEOUT);
       if (st) *(volatile int*)&st->stop = 3;
+      sweep_drain(bar, lbar, a.ring, ready, next, slot_w, par_w, lwaited, lstaged);
     }
-    if (warp == 0 && lane == 0) {
-      for (; ready < next - 1; ++ready) {
-        (void)mbar_wait_bounded(&bar[slot_w], par_w);
-        if (++slot_w == a.ring) {
-          slot_w = 0;
-          par_w ^= 1u;
-        }
-      }
-    }
-    if (tid == 0)  // list copies staged but not yet seen landing
-      for (int b = lwaited; b < lstaged; ++b) (void)mbar_wait_bounded(&lbar[b % SW_LR], (unsigned)(b / SW_LR) & 1u);
     __syncthreads();
+    return;
   }
+  cp_async_wait_all();
 }
 
 // per-row diagonal data of pass 2 (renumbered tables)
@@ -205,22 +232,20 @@ struct SweepDiag {
 
 // the epilogue's global inputs of one target column block, for one thread
 struct SweepPre {
-  int64_t s0, s1;    // S of the thread's two rows
+  int64_t s;         // S of the thread's row
   uint64_t sd;       // dn state
   int64_t ed;        // dn energy (int32 or fixed point)
 };
 
 template <bool DIAG64>
 __device__ __forceinline__ SweepPre sweep_prefetch(const SweepDiag& dg, const int64_t* W, int64_t nd, int64_t u0,
-                                                   int er0, int er1, bool rv0, bool rv1, int64_t j, int lane,
-                                                   int nblk, uint64_t pol) {
-  SweepPre p{0, 0, 0, 0};
+                                                   int er, bool rv, int64_t j, int lane, int nblk, uint64_t pol) {
+  SweepPre p{0, 0, 0};
   const int64_t d = j * SW_CH + lane;
   if (j < nblk && d < nd) {
     p.sd = __ldg(dg.s_dn + d);
     p.ed = DIAG64 ? __ldg(dg.f_dn + d) : (int64_t)__ldg(dg.e_dn + d);
-    if (rv0) p.s0 = ld_keep(W + (u0 + er0) * nd + d, pol);
-    if (rv1) p.s1 = ld_keep(W + (u0 + er1) * nd + d, pol);
+    if (rv) p.s = ld_keep(W + (u0 + er) * nd + d, pol);
   }
   return p;
 }
@@ -245,23 +270,24 @@ __global__ void __launch_bounds__(SW_NT, 2)
   const int64_t u0 = (int64_t)blockIdx.x * SW_W;
   const int nrows = (int)min((int64_t)SW_W, a.nu - u0);
   const int64_t nchunks = (a.nd + SW_CH - 1) / SW_CH;
-  for (int i = tid; i < a.ring; i += SW_NT) mbar_init(&bar[i], SW_NT);
-  for (int i = tid; i < SW_LR; i += SW_NT) mbar_init(&lbar[i], 1);
   int lstaged = 0;   // list blocks staged (thread 0)
   int lwaited = 0;   // list blocks whose copy this thread has seen land
   if (tid == 0) {
+    // one thread initialises every barrier and fences its inits (see pass 1)
+    for (int i = 0; i < a.ring; ++i) mbar_init(&bar[i], SW_NT);
+    for (int i = 0; i < SW_LR; ++i) mbar_init(&lbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     for (; lstaged < SW_LR && lstaged < a.nblk; ++lstaged) sweep_stage_lists(a.lst, a.nd, lstaged, lring, lbar, lstaged);
   }
   __syncthreads();
   const uint64_t pol_x = sweep_policy(a.pol, 0), pol_w = sweep_policy(a.pol, 1), pol_s = policy_evict_first();
-  // the epilogue rows of this thread (warp and warp + 8) and their diagonal data
-  const int er0 = warp, er1 = warp + 8;
-  const bool rv0 = er0 < nrows, rv1 = er1 < nrows;
-  const int64_t eu_row0 = rv0 ? u0 + er0 : u0, eu_row1 = rv1 ? u0 + er1 : u0;
-  const uint64_t su0 = __ldg(dg.s_up + eu_row0), su1 = __ldg(dg.s_up + eu_row1);
-  const int64_t eu0 = DIAG64 ? 0 : (int64_t)__ldg(dg.e_up + eu_row0), eu1 = DIAG64 ? 0 : (int64_t)__ldg(dg.e_up + eu_row1);
-  const int64_t ef0 = DIAG64 ? __ldg(dg.f_up + eu_row0) : 0, ef1 = DIAG64 ? __ldg(dg.f_up + eu_row1) : 0;
+  // the epilogue row of this thread (= warp) and its diagonal data
+  const int er = warp;
+  const bool rv = er < nrows;
+  const int64_t eu_row = rv ? u0 + er : u0;
+  const uint64_t su = __ldg(dg.s_up + eu_row);
+  const int64_t eu = DIAG64 ? 0 : (int64_t)__ldg(dg.e_up + eu_row);
+  const int64_t ef = DIAG64 ? __ldg(dg.f_up + eu_row) : 0;
   int64_t next = 0;
   int slot_i = 0;
   int64_t ready = -1;
@@ -273,24 +299,22 @@ __global__ void __launch_bounds__(SW_NT, 2)
   unsigned long long mx = 0;
   const int rr = lane & 15, half = lane >> 4;
   // epilogue inputs two blocks ahead, the window one block ahead
-  SweepPre pre0 = sweep_prefetch<DIAG64>(dg, W, a.nd, u0, er0, er1, rv0, rv1, 0, lane, a.nblk, pol_s);
-  SweepPre pre1 = sweep_prefetch<DIAG64>(dg, W, a.nd, u0, er0, er1, rv0, rv1, 1, lane, a.nblk, pol_s);
+  SweepPre pre0 = sweep_prefetch<DIAG64>(dg, W, a.nd, u0, er, rv, 0, lane, a.nblk, pol_s);
+  SweepPre pre1 = sweep_prefetch<DIAG64>(dg, W, a.nd, u0, er, rv, 1, lane, a.nblk, pol_s);
   int2 w_next = __ldg(&a.win[0]);
   for (int j = 0; j < a.nblk; ++j) {
     const int2 w = w_next;
     if (j + 1 < a.nblk) w_next = __ldg(&a.win[j + 1]);
     const SweepPre cur = pre0;
     pre0 = pre1;
-    pre1 = sweep_prefetch<DIAG64>(dg, W, a.nd, u0, er0, er1, rv0, rv1, j + 2, lane, a.nblk, pol_s);
+    pre1 = sweep_prefetch<DIAG64>(dg, W, a.nd, u0, er, rv, j + 2, lane, a.nblk, pol_s);
     const int ls = j % SW_LR;
     // refill (every thread copies two elements of each new chunk, then arrives)
     const int64_t lim = min(nchunks - 1, (int64_t)w.x + a.ring - 1);
     for (; next <= lim; ++next) {
       const int64_t cc0 = next * SW_CH;
-#pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const int e = tid + k * SW_NT;
-        const int r = e >> 5, c = e & 31;
+      {
+        const int r = tid >> 5, c = tid & 31;  // 16 rows x 32 columns: one element per thread
         if (r < nrows && cc0 + c < a.nd)
           cp_async8(win + (size_t)r * RS + slot_i * SW_CH + c, X + (u0 + r) * a.nd + cc0 + c, pol_x);
       }
@@ -314,29 +338,13 @@ __global__ void __launch_bounds__(SW_NT, 2)
       bad = true;
       break;
     }
-    // gather: half-warp = one target column, lane = row
-    const uint16_t* lb = lring + (size_t)ls * SW_CH * SW_LST;
-#pragma unroll
-    for (int q = 0; q < SW_CH / 16; ++q) {
-      const int cl = 16 * q + 2 * warp + half;
+    // gather: half-warp = one target column of the block, lane = row of the stripe
+    {
+      const int cl = 2 * warp + half;
       const int64_t d = (int64_t)j * SW_CH + cl;
-      int64_t hp = 0, hn = 0;
-      if (d < a.nd) {
-        const uint4* lp = (const uint4*)(lb + cl * SW_LST);
-        const uint4 L0 = lp[0], L1 = lp[1];
-        const uint32_t wd[8] = {L0.x, L0.y, L0.z, L0.w, L1.x, L1.y, L1.z, L1.w};
-        const int cnt = (int)(wd[7] >> 16);
-        const int64_t* wr = win + (size_t)rr * RS;
-#pragma unroll
-        for (int e = 0; e < SW_LST - 1; ++e) {
-          if (e < cnt) {
-            const uint32_t en = SW_ENTRY(wd, e);
-            const int64_t v = wr[en & 0x7fffu];
-            if (en & 0x8000u) hn += v; else hp += v;
-          }
-        }
-      }
-      stage[rr * (SW_CH + 1) + cl] = hp - hn;
+      const int64_t hsum =
+          d < a.nd ? sweep_hops<1>(win + (size_t)rr * RS, lring + ((size_t)ls * SW_CH + cl) * SW_LST) : 0;
+      stage[rr * (SW_CH + 1) + cl] = hsum;
     }
     __syncthreads();
     if (tid == 0 && j + SW_LR < a.nblk) {
@@ -344,25 +352,18 @@ __global__ void __launch_bounds__(SW_NT, 2)
       sweep_stage_lists(a.lst, a.nd, j + SW_LR, lring, lbar, ls);
       ++lstaged;
     }
-    // epilogue: row er0 / er1, column j*32 + lane
+    // epilogue: row er (= warp), column j*32 + lane
     {
       const int64_t d = (int64_t)j * SW_CH + lane;
-      if (d < a.nd) {
+      if (d < a.nd && rv) {
         const int32_t ed32 = DIAG64 ? 0 : (int32_t)cur.ed;
         const int64_t ed64 = DIAG64 ? cur.ed : 0;
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          const int r = k ? er1 : er0;
-          if (k ? rv1 : rv0) {
-            const int64_t x = win[(size_t)r * RS + jslot * SW_CH + lane];
-            const int64_t ww = (int64_t)h.t_int * ((k ? cur.s1 : cur.s0) + stage[r * (SW_CH + 1) + lane]) +
-                               bfp_diag_col<DIAG64>(h, k ? eu1 : eu0, k ? ef1 : ef0, k ? su1 : su0, cur.sd, ed32, ed64,
-                                                    x);
-            st_stream(W + (u0 + r) * a.nd + d, ww, pol_w);
-            add128(dot, mul_s64(x, ww));
-            mx = max(mx, uabs64(ww));
-          }
-        }
+        const int64_t x = win[(size_t)er * RS + jslot * SW_CH + lane];
+        const int64_t ww = (int64_t)h.t_int * (cur.s + stage[er * (SW_CH + 1) + lane]) +
+                           bfp_diag_col<DIAG64>(h, eu, ef, su, cur.sd, ed32, ed64, x);
+        st_stream(W + (u0 + er) * a.nd + d, ww, pol_w);
+        add128(dot, mul_s64(x, ww));
+        mx = max(mx, uabs64(ww));
       }
     }
     if (++jslot == a.ring) jslot = 0;
@@ -374,15 +375,7 @@ __global__ void __launch_bounds__(SW_NT, 2)
     if (tid == 0) {
       record_status(status, DEV_TIMEOUT);
       if (st) *(volatile int*)&st->stop = 3;
-      // and the arrivals those copies trigger have reached the barriers (bounded)
-      for (; ready < next - 1; ++ready) {
-        (void)mbar_wait_bounded(&bar[slot_w], par_w);
-        if (++slot_w == a.ring) {
-          slot_w = 0;
-          par_w ^= 1u;
-        }
-      }
-      for (int b = lwaited; b < lstaged; ++b) (void)mbar_wait_bounded(&lbar[b % SW_LR], (unsigned)(b / SW_LR) & 1u);
+      sweep_drain(bar, lbar, a.ring, ready, next, slot_w, par_w, lwaited, lstaged);
     }
     __syncthreads();
     return;

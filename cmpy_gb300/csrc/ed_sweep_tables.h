@@ -13,10 +13,10 @@
 
 namespace ed {
 
-constexpr int SW_NT = 256;   // threads per CTA of both passes
+constexpr int SW_NT = 512;   // threads per CTA of both passes (one target row / column per half-warp)
 constexpr int SW_CH = 32;    // rows (pass 1) / columns (pass 2) per ring chunk and per target block
 constexpr int SW_W = 16;     // stripe width: columns (pass 1) / rows (pass 2) per CTA
-constexpr int SW_LST = 16;   // uint16 entries per hop list (15 partners + count)
+constexpr int SW_LST = 16;   // uint16 entries per hop list (15 partners + counts)
 
 // ---- host: renumbering, hop lists, ring windows ------------------------------------------------
 
@@ -173,7 +173,7 @@ static bool sweep_order(int64_t n, const std::vector<int32_t>& off, const std::v
 }
 
 // hop lists of the renumbered targets: ring offsets of the partners for a ring of `ring`
-// chunks, 0x8000 marking a negative coefficient, entry 15 = count
+// chunks, entries with a positive coefficient first; entry 15 = count | (positive count << 8)
 static void sweep_lists(int64_t n, const std::vector<int32_t>& off, const std::vector<int32_t>& idx,
                         const std::vector<double>& coef, int ring, SweepSide* out) {
   std::vector<int32_t> inv(n);
@@ -184,12 +184,14 @@ static void sweep_lists(int64_t n, const std::vector<int32_t>& off, const std::v
   for (int64_t i = 0; i < n; ++i) {
     const int64_t v = out->perm[i];
     uint16_t* L = out->lst.data() + (size_t)i * SW_LST;
-    int c = 0;
-    for (int32_t k = off[v]; k < off[v + 1]; ++k) {
-      if (coef[k] == 0.0) continue;
-      L[c++] = (uint16_t)((inv[idx[k]] % ring_elems) | (coef[k] < 0.0 ? 0x8000u : 0u));
-    }
-    L[SW_LST - 1] = (uint16_t)c;
+    int c = 0, npos = 0;
+    for (int sign = 1; sign >= -1; sign -= 2)
+      for (int32_t k = off[v]; k < off[v + 1]; ++k) {
+        if (coef[k] == 0.0 || (coef[k] > 0.0) != (sign > 0)) continue;
+        L[c++] = (uint16_t)(inv[idx[k]] % ring_elems);
+        if (sign > 0) ++npos;
+      }
+    L[SW_LST - 1] = (uint16_t)(c | (npos << 8));
   }
 }
 

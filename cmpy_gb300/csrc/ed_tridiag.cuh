@@ -187,6 +187,56 @@ static __device__ double tridiag_lowest_block(const double* a_g, const double* b
   return ev;
 }
 
+// v = -(T - e0)^+ r on the complement of c (c the unit eigenvector of T for its lowest
+// eigenvalue e0), the tridiagonal part of the adjoint of that eigenpair. Thread 0: the shifted
+// system (T - (e0 - delta)) y = r - (r.c) c by Gaussian elimination with partial pivoting, then
+// v = -(y - (y.c) c). delta = 1e-13 max(1, |e0|) keeps the factorisation regular; off c it
+// changes the solution by a relative delta / (gap to the next eigenvalue). work: 5*m doubles.
+static __device__ void tridiag_pinv_solve(const double* a, const double* b, int m, double e0, const double* c,
+                                          const double* r, double* v, double* work) {
+  if (threadIdx.x != 0) return;
+  double rc = 0.0;
+  for (int i = 0; i < m; ++i) rc = fma(r[i], c[i], rc);
+  for (int i = 0; i < m; ++i) v[i] = r[i] - rc * c[i];
+  const double shift = e0 - 1e-13 * fmax(1.0, fabs(e0));
+  double* dd = work;           // diagonal of U
+  double* du = work + m;       // first super-diagonal of U
+  double* du2 = work + 2 * m;  // second super-diagonal of U
+  double* ml = work + 3 * m;   // multipliers
+  double* pv = work + 4 * m;   // 1.0 if rows swapped at step i
+  for (int i = 0; i < m; ++i) { dd[i] = a[i] - shift; du[i] = (i + 1 < m) ? b[i + 1] : 0.0; du2[i] = 0.0; }
+  for (int i = 0; i < m - 1; ++i) {
+    const double sub = b[i + 1];
+    if (fabs(dd[i]) >= fabs(sub)) {
+      pv[i] = 0.0;
+      ml[i] = dd[i] != 0.0 ? sub / dd[i] : 0.0;
+      dd[i + 1] -= ml[i] * du[i];
+    } else {
+      pv[i] = 1.0;
+      const double l = dd[i] / sub, t0 = dd[i + 1], t1 = (i + 2 < m) ? du[i + 1] : 0.0, odu = du[i];
+      ml[i] = l;
+      dd[i] = sub;
+      du[i] = t0;
+      du2[i] = t1;
+      dd[i + 1] = odu - l * t0;
+      if (i + 2 < m) du[i + 1] = -l * t1;
+    }
+  }
+  for (int i = 0; i < m - 1; ++i) {
+    if (pv[i] != 0.0) { const double t = v[i]; v[i] = v[i + 1]; v[i + 1] = t - ml[i] * v[i]; }
+    else v[i + 1] -= ml[i] * v[i];
+  }
+  for (int i = m - 1; i >= 0; --i) {
+    double t = v[i];
+    if (i + 1 < m) t -= du[i] * v[i + 1];
+    if (i + 2 < m) t -= du2[i] * v[i + 2];
+    v[i] = dd[i] != 0.0 ? t / dd[i] : 0.0;
+  }
+  double yc = 0.0;
+  for (int i = 0; i < m; ++i) yc = fma(v[i], c[i], yc);
+  for (int i = 0; i < m; ++i) v[i] = -(v[i] - yc * c[i]);
+}
+
 // ---- the same on the host ----------------------------------------------------------------------
 // Lowest eigenpair of the tridiagonal (a[0..m), b[1..m)) on the host, FP64: bisection on the
 // Sturm count of the LDL^T pivots, then two steps of inverse iteration (Gaussian elimination

@@ -26,6 +26,8 @@ __all__ = [
     "lanczos",
     "lanczos_coeffs",
     "tridiag_lowest",
+    "tridiag_lowest_batch",
+    "tridiag_pinv_solve_batch",
     "continued_fraction",
     "lehmann_accumulate",
     "csr_matvec",
@@ -226,8 +228,9 @@ class Plan:
 
     @property
     def matvec_variant(self) -> int:
-        """Fixed-point matvec the plan uses: 5 = banded two-pass sweep (renumbered basis inside
-        the Lanczos), 3/2/1 = single-pass kernels, 0 = none (FP64 matvec)."""
+        """Fixed-point matvec the plan uses: 3/2/1 = single-pass kernels, 5 = banded two-pass
+        sweep (renumbered basis inside the Lanczos; only when forced or where 3 does not fit),
+        0 = none (FP64 matvec)."""
         return int(N.lib().ed_plan_matvec_variant(self._h))
 
     def set_matvec_variant(self, variant: int) -> None:
@@ -236,7 +239,7 @@ class Plan:
 
     def set_wait_limit(self, polls: int) -> None:
         """Polls of a first bulk-copy wait in the fixed-point matvec before it gives up and the
-        solve reports ED_ERR_TIMEOUT (0 = default)."""
+        solve reports ED_ERR_TIMEOUT (0 = default, -1 = give up without polling)."""
         N.check(N.lib().ed_plan_set_wait_limit(self._h, int(polls)))
 
     def matvec_fixed(self, xm: torch.Tensor, ex: int) -> tuple[torch.Tensor, int]:
@@ -477,6 +480,40 @@ def tridiag_lowest(alpha, beta, want_vector: bool = True):
     vec = torch.empty(m, dtype=torch.float64, device=device()) if want_vector else None
     N.check(N.lib().ed_tridiag_lowest(N.ptr(a), N.ptr(b), m, N.ptr(val), N.ptr(vec), _stream()))
     return float(val.item()), vec
+
+
+def tridiag_lowest_batch(alpha: torch.Tensor, beta: torch.Tensor, m) -> tuple[torch.Tensor, torch.Tensor]:
+    """Lowest eigenpairs of B tridiagonals in one launch: alpha [B, lda], beta [B, ldb] (row b
+    uses alpha[b, :m[b]], beta[b, 1:m[b]]). Returns (values [B], vectors [B, lda]) on the device."""
+    a = _as_dev_f64(alpha).contiguous()
+    b = _as_dev_f64(beta).contiguous()
+    B, lda = a.shape
+    mm = torch.as_tensor(np.asarray(m, dtype=np.int32)).to(device())
+    max_m = int(np.max(np.asarray(m))) if B else 1
+    vals = torch.empty(B, dtype=torch.float64, device=device())
+    vecs = torch.zeros((B, lda), dtype=torch.float64, device=device())
+    N.check(N.lib().ed_tridiag_lowest_batch(N.ptr(a), lda, N.ptr(b), b.shape[1], N.ptr(mm), B, max_m, N.ptr(vals),
+                                            N.ptr(vecs), lda, _stream()))
+    return vals, vecs
+
+
+def tridiag_pinv_solve_batch(alpha: torch.Tensor, beta: torch.Tensor, m, e0: torch.Tensor, c: torch.Tensor,
+                             rhs: torch.Tensor) -> torch.Tensor:
+    """v_b = -(T_b - e0_b)^+ rhs_b on the complement of c_b for B tridiagonals (c_b the unit
+    lowest eigenvector of T_b, e0_b its eigenvalue); rows as in tridiag_lowest_batch."""
+    a = _as_dev_f64(alpha).contiguous()
+    b = _as_dev_f64(beta).contiguous()
+    cc = _as_dev_f64(c).contiguous()
+    r = _as_dev_f64(rhs).contiguous()
+    e = _as_dev_f64(e0).contiguous()
+    B = a.shape[0]
+    mm = torch.as_tensor(np.asarray(m, dtype=np.int32)).to(device())
+    max_m = int(np.max(np.asarray(m))) if B else 1
+    out = torch.zeros_like(r)
+    N.check(N.lib().ed_tridiag_pinv_solve_batch(N.ptr(a), a.shape[1], N.ptr(b), b.shape[1], N.ptr(mm), B, max_m,
+                                                N.ptr(e), N.ptr(cc), cc.shape[1], N.ptr(r), N.ptr(out), r.shape[1],
+                                                _stream()))
+    return out
 
 
 def _as_dev_c128(z) -> torch.Tensor:

@@ -280,6 +280,21 @@ ED_API ed_status ed_lanczos_coeffs(ed_plan plan, int max_steps, const double* d_
  * d_vec (FP64[m]) may be NULL. */
 ED_API ed_status ed_tridiag_lowest(const double* d_alpha, const double* d_beta, int m,
                                    double* d_value, double* d_vec, ed_stream_t stream);
+/* The same for B tridiagonals in one launch (one block each): problem b is alpha[b*lda ..],
+ * beta[b*ldb ..] of size d_m[b] <= max_m (device int array); eigenvalue -> d_values[b],
+ * eigenvector -> d_vecs[b*ldv ..]. Used by the adjoint Green's function for the ground state
+ * of each taped Lanczos run (the reference's eigh_tridiagonal, cmpy/exactdiag.py:368-375). */
+ED_API ed_status ed_tridiag_lowest_batch(const double* d_alpha, int lda, const double* d_beta, int ldb,
+                                         const int* d_m, int B, int max_m, double* d_values, double* d_vecs,
+                                         int ldv, ed_stream_t stream);
+/* v_b = -(T_b - e0_b)^+ r_b on the complement of c_b, for B tridiagonals (c_b the unit
+ * eigenvector of T_b's lowest eigenvalue e0_b, d_e0 on the device): the tridiagonal part of the
+ * reverse pass through a Lanczos ground state. No reference counterpart (cmpy has no
+ * derivatives). d_rhs and d_out must not alias. */
+ED_API ed_status ed_tridiag_pinv_solve_batch(const double* d_alpha, int lda, const double* d_beta, int ldb,
+                                             const int* d_m, int B, int max_m, const double* d_e0,
+                                             const double* d_c, int ldc, const double* d_rhs, double* d_out,
+                                             int ldr, ed_stream_t stream);
 
 /* ---- batched form: many sectors / realisations in one persistent launch -----------------
  * No reference counterpart: the reference solves sectors one after another on the host
@@ -440,11 +455,12 @@ ED_API ed_status ed_fixed_to_f64(const int64_t* d_xm, int64_t n, int32_t exp, do
  * ed_plan_fixed_point, also returned in *h_m_in), output exponent *h_ew = ex - F. */
 ED_API ed_status ed_matvec_fixed(ed_plan plan, const int64_t* d_xm, int32_t ex, int64_t* d_wm,
                                  int32_t* h_ew, int* h_m_in, ed_stream_t stream);
-/* Which fixed-point matvec the plan uses (0: none). 5 is the banded two-pass sweep: the plan
- * renumbers the up and the dn states (reverse Cuthill-McKee order of each spin's hop graph)
- * and its Lanczos runs keep their vectors in that basis; ed_matvec_fixed still takes and
- * returns vectors in the sector's ascending-state order. 3, 2, 1: single-pass kernels. The
- * environment variable CMPY_ED_MATVEC=1..5 forces a variant where the sector allows it. */
+/* Which fixed-point matvec the plan uses (0: none). 3, 2, 1: single-pass kernels (3 where the
+ * sector fits it). 5 is the banded two-pass sweep, chosen only when forced or where 3 does not
+ * fit: the plan renumbers the up and the dn states (reverse Cuthill-McKee order of each spin's
+ * hop graph) and its Lanczos runs keep their vectors in that basis; ed_matvec_fixed still takes
+ * and returns vectors in the sector's ascending-state order. The environment variable
+ * CMPY_ED_MATVEC=1..5 forces a variant where the sector allows it. */
 ED_API int ed_plan_matvec_variant(ed_plan plan);
 /* Chooses the fixed-point matvec variant of this plan (0: automatic, 1..5 as above when the
  * sector allows it, else the automatic choice); for comparisons and benchmarks. Takes effect
@@ -452,7 +468,8 @@ ED_API int ed_plan_matvec_variant(ed_plan plan);
 ED_API ed_status ed_plan_set_matvec_variant(ed_plan plan, int variant);
 /* Polls of a first wait for a bulk copy in the fixed-point matvec before the kernel gives up
  * (records ED_ERR_TIMEOUT in the solve, lets its copies land and returns); 0 restores the
- * default (2^22 polls). A small limit lets tests exercise the give-up path. */
+ * default (2^22 polls); -1 makes the first wait give up without polling, which lets tests
+ * exercise the give-up path. */
 ED_API ed_status ed_plan_set_wait_limit(ed_plan plan, int64_t polls);
 
 /* Allocation-free ed_tridiag_lowest (no counterpart in the reference). For callers that

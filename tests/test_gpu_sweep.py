@@ -1,11 +1,12 @@
 """GPU parity of the banded two-pass fixed-point matvec (variant 5, the "sweep").
 
-* it is chosen for the benchmark sectors and its integer H·x equals the single-pass kernel's
-  (variant 3) bit for bit, and the oracle's integer matrix on small sectors, for exact and
+* it is available on the benchmark sectors (the plans choose the faster single-pass kernel,
+  variant 3, by default) and its integer H·x equals variant 3's bit for bit, and the oracle's integer matrix on small sectors, for exact and
   rounded (arbitrary on-site energy) diagonals;
 * a Lanczos run in its renumbered basis gives the same coefficients and ground state as the
   single-pass run, and the 12-site ring's ground-state energy measured on the reference;
-* a first wait that gives up reports ED_ERR_TIMEOUT, and the next call on the plan succeeds.
+* a first wait that gives up (wait limit -1: no polling) reports ED_ERR_TIMEOUT, and the next
+  call on the plan succeeds.
 """
 
 import numpy as np
@@ -44,15 +45,16 @@ CASES = [
 @pytest.mark.parametrize("name,mk,sec", CASES, ids=[c[0] for c in CASES])
 def test_sweep_bitexact_vs_single_pass(cuda, name, mk, sec):
     p = mk().plan(*sec)
-    assert p.matvec_variant == 5, name
+    assert p.matvec_variant == 3, name
     xm = _rand_mantissas(p, 7)
-    w5, e5 = p.matvec_fixed(xm, -10)
-    p.set_matvec_variant(3)
+    w3, e3 = p.matvec_fixed(xm, -10)
+    p.set_matvec_variant(5)
     try:
-        assert p.matvec_variant == 3
-        w3, e3 = p.matvec_fixed(xm, -10)
+        assert p.matvec_variant == 5
+        w5, e5 = p.matvec_fixed(xm, -10)
     finally:
         p.set_matvec_variant(0)
+    assert p.matvec_variant == 3
     assert e5 == e3
     assert torch.equal(w5, w3), (name, int((w5 != w3).sum()))
 
@@ -62,6 +64,7 @@ def test_sweep_vs_oracle_integer_matrix(cuda, nu, nd):
     """Dyadic sector (t = 1/2, U = 3): the integer matvec equals the oracle's H * 2^F."""
     m = _hub(8, True, inter=3.0, mu=1.5, hop=0.5)
     p = m.plan(nu, nd)
+    p.set_matvec_variant(5)
     assert p.matvec_variant == 5
     eps, u, bonds, width = m.fermion_descriptor()
     up, dn = O.sector_states(8, nu), O.sector_states(8, nd)
@@ -82,17 +85,18 @@ def test_sweep_lanczos_matches_single_pass(cuda):
     from cmpy_gb300 import engine as E
 
     p = _hub(12, True, inter=4.0, mu=2.0).plan(6, 6)
-    assert p.matvec_variant == 5
     g = torch.Generator(device="cuda").manual_seed(12)
     v0 = torch.rand(p.dim, dtype=torch.float64, device="cuda", generator=g)
     # once the ground state has converged (~100 steps here), a Lanczos run without
     # reorthogonalisation turns rounding differences (here the reduction order of the dot
     # products) into different ghost copies: compare the coefficients before that
     kw = dict(max_steps=200, want_vector=True, v0=v0, tol=1e-12, check_every=10)
-    r5 = E.lanczos(p, **kw)
-    p.set_matvec_variant(3)
+    assert p.matvec_variant == 3
+    r3 = E.lanczos(p, **kw)
+    p.set_matvec_variant(5)
     try:
-        r3 = E.lanczos(p, **kw)
+        assert p.matvec_variant == 5
+        r5 = E.lanczos(p, **kw)
     finally:
         p.set_matvec_variant(0)
     assert r5.steps == r3.steps
@@ -108,7 +112,7 @@ def test_sweep_lanczos_matches_single_pass(cuda):
 
 @pytest.mark.parametrize("variant", [5, 3])
 def test_first_wait_gives_up_then_recovers(cuda, variant):
-    """A wait limit of one poll: the matvec's first wait for its bulk copies gives up, the
+    """Wait limit -1: the matvec's first wait for its copies gives up without polling, the
     kernel lets its copies land and returns, the solve reports ED_ERR_TIMEOUT; with the
     default limit the next solve on the same plan succeeds."""
     from cmpy_gb300 import _native as N
@@ -118,7 +122,7 @@ def test_first_wait_gives_up_then_recovers(cuda, variant):
     p.set_matvec_variant(variant)
     try:
         assert p.matvec_variant == variant
-        p.set_wait_limit(1)
+        p.set_wait_limit(-1)
         with pytest.raises(N.EDError) as ei:
             E.lanczos(p, max_steps=40, want_vector=False)
         assert ei.value.status == N.ED_ERR_TIMEOUT
