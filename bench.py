@@ -57,9 +57,9 @@ def parse():
 
 
 def run_matvec_only(n: int):
-    """N fixed-point Lanczos steps of the 14-site (7,7) sector per matvec variant (5 = banded
-    two-pass sweep, 3 = single-pass), the matvec launches timed with CUDA events on the
-    launching stream (one JSON line per variant)."""
+    """N fixed-point Lanczos steps of the 14-site (7,7) sector per matvec variant (6 = two-pass
+    stripes, 5 = banded two-pass sweep, 3 = single-pass), the matvec launches timed with CUDA
+    events on the launching stream (one JSON line per variant)."""
     import torch
 
     from cmpy_gb300 import engine as E
@@ -68,7 +68,8 @@ def run_matvec_only(n: int):
     plan = E.Plan.fermion(N_SITES, [-MU] * N_SITES, [U] * N_SITES, bonds, N_UP, N_DN)
     v0 = torch.rand(plan.dim, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(5))
     peak, _ = peaks()
-    for var in (5, 3):
+    kernels = {6: "k_stripe_up + k_stripe_dn", 5: "k_sweep_up + k_sweep_dn", 3: "k_bfp_hub_matvec3"}
+    for var in (6, 5, 3):
         plan.set_matvec_variant(var)
         if plan.matvec_variant != var:
             continue
@@ -76,7 +77,7 @@ def run_matvec_only(n: int):
         r = E.lanczos(plan, max_steps=n, want_vector=False, v0=v0, profile=True)
         us = 1e3 * r.matvec_ms / max(r.matvecs, 1)
         gbs = 16.0 * plan.dim / (us * 1e-6) / 1e9
-        print(json.dumps({"variant": var, "kernels": "k_sweep_up + k_sweep_dn" if var == 5 else "k_bfp_hub_matvec3",
+        print(json.dumps({"variant": var, "kernels": kernels[var],
                           "dim": plan.dim, "matvecs": r.matvecs, "matvec_us": round(us, 2), "gbs": round(gbs, 1),
                           "frac": round(gbs / peak, 4), "alpha0": float(r.alpha[0]), "energy": r.energy}), flush=True)
     plan.set_matvec_variant(0)

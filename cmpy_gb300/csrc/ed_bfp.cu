@@ -20,6 +20,7 @@
 
 #include "ed_lzcheck.cuh"
 #include "ed_plan.cuh"
+#include "ed_stripe_tables.h"
 #include "ed_sweep_tables.h"
 #include "ed_tridiag.cuh"
 
@@ -840,6 +841,7 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
 }
 
 #include "ed_sweep.cuh"
+#include "ed_stripe.cuh"
 
 // ---- two-pass H·v, pass 1: up-neighbour sums by column panels ---------------------------------
 // The up-hop part of H·v, W[u, c] = sum_{u'} (+-) X[u', c], is a sparse-times-dense product. A
@@ -1057,8 +1059,8 @@ __global__ void __launch_bounds__(BT, 4) k_bfp_update(BfpVecs v, int k, const in
 
 // ---- Ritz vector ------------------------------------------------------------------------------------
 // psi = sum_k C_k R_k * 2^-SC (C_k and SC from the host: see bfp_lanczos)
-// (pu, pd non-null: the vectors are in the renumbered basis of the sweep matvec and psi is
-// scattered back to the original order, nd = num_dn)
+// (pu, pd non-null: the vectors are in the renumbered basis of the sweep or the stripe matvec
+// and psi is scattered back to the original order, nd = num_dn)
 __global__ void k_bfp_ritz(const BfpVecs v, const int64_t* __restrict__ C, const int* SCp, const BfpState* st,
                            double* __restrict__ out, const int32_t* __restrict__ pu, const int32_t* __restrict__ pd,
                            int64_t nd) {
@@ -1114,6 +1116,98 @@ static size_t sweep_smem_dn(int r) {
          (size_t)SW_LR * (SW_CH * SW_LST * 2 + 8);
 }
 
+// device copy of a host array (at least 8 bytes allocated)
+static ed_status dev_upload(void** dst, const void* src, size_t bytes, cudaStream_t s) {
+  ED_CUDA(cudaMalloc(dst, std::max<size_t>(bytes, 8)));
+  if (bytes) ED_CUDA(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, s));
+  return ED_OK;
+}
+
+// device copies of both species' diagonal data (states and per-state energies of the plan's
+// diagonal mode) in a renumbered order (pu, pd: new -> old); synchronous
+static ed_status upload_renumbered_diag(const ed_plan_s* p, const BfpTables& B, const std::vector<int32_t>& pu,
+                                        const std::vector<int32_t>& pd, const std::vector<int32_t>& eui,
+                                        const std::vector<int32_t>& edi, const std::vector<int64_t>& euf,
+                                        const std::vector<int64_t>& edf, uint64_t** s_up, uint64_t** s_dn,
+                                        int32_t** e_up, int32_t** e_dn, int64_t** f_up, int64_t** f_dn,
+                                        cudaStream_t s) {
+  const int64_t nu = p->num_up, nd = p->num_dn;
+  std::vector<uint64_t> st_up(nu), st_dn(nd), sup(nu), sdn(nd);
+  ED_CUDA(cudaMemcpyAsync(st_up.data(), p->up.states, nu * 8, cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(st_dn.data(), p->dn.states, nd * 8, cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  for (int64_t i = 0; i < nu; ++i) sup[i] = st_up[pu[i]];
+  for (int64_t i = 0; i < nd; ++i) sdn[i] = st_dn[pd[i]];
+  ED_TRY(dev_upload((void**)s_up, sup.data(), sup.size() * 8, s));
+  ED_TRY(dev_upload((void**)s_dn, sdn.data(), sdn.size() * 8, s));
+  if (!B.diag64) {
+    std::vector<int32_t> a(nu), b(nd);
+    for (int64_t i = 0; i < nu; ++i) a[i] = eui[pu[i]];
+    for (int64_t i = 0; i < nd; ++i) b[i] = edi[pd[i]];
+    ED_TRY(dev_upload((void**)e_up, a.data(), a.size() * 4, s));
+    ED_TRY(dev_upload((void**)e_dn, b.data(), b.size() * 4, s));
+    ED_CUDA(cudaStreamSynchronize(s));
+  } else {
+    std::vector<int64_t> a(nu), b(nd);
+    for (int64_t i = 0; i < nu; ++i) a[i] = euf[pu[i]];
+    for (int64_t i = 0; i < nd; ++i) b[i] = edf[pd[i]];
+    ED_TRY(dev_upload((void**)f_up, a.data(), a.size() * 8, s));
+    ED_TRY(dev_upload((void**)f_dn, b.data(), b.size() * 8, s));
+    ED_CUDA(cudaStreamSynchronize(s));
+  }
+  return ED_OK;
+}
+
+// Tables of the stripe matvec (ed_stripe.cuh); leaves B.sp.on = 0 when the sector does not
+// suit it (a target with more than 2 ST_PMAX - 2 hops, a stripe larger than one CTA's shared
+// memory). CMPY_ED_STRIPE=0 disables it.
+static ed_status build_stripe(ed_plan_s* p, BfpTables& B, const std::vector<int32_t>& uoff,
+                              const std::vector<int32_t>& uidx, const std::vector<double>& ucoef,
+                              const std::vector<int32_t>& doff, const std::vector<int32_t>& didx,
+                              const std::vector<double>& dcoef, const std::vector<int32_t>& eui,
+                              const std::vector<int32_t>& edi, const std::vector<int64_t>& euf,
+                              const std::vector<int64_t>& edf, cudaStream_t s) {
+  StripeTables& T = B.sp;
+  T = StripeTables();
+  const char* env = getenv("CMPY_ED_STRIPE");
+  if (env && atoi(env) == 0) return ED_OK;
+  const int64_t nu = p->num_up, nd = p->num_dn;
+  // CTAs per SM: two when a stripe buffer fits in half of the SM's shared memory
+  int per_sm = 0;
+  ED_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, p->device));
+  const size_t two = (size_t)per_sm / 2 - 1024 - 512, one = (size_t)p->ctx->smem_optin - 512;
+  auto ctas = [&](int64_t n) { return stripe_smem(n) <= two ? 2 : (stripe_smem(n) <= one ? 1 : 0); };
+  T.per_sm_up = ctas(nu);
+  T.per_sm_dn = ctas(nd);
+  if (T.per_sm_up == 0 || T.per_sm_dn == 0) return ED_OK;
+  StripeSide su, sd;
+  if (!stripe_order(nu, uoff, uidx, ucoef, &su) || !stripe_order(nd, doff, didx, dcoef, &sd)) return ED_OK;
+  ED_TRY(upload_renumbered_diag(p, B, su.perm, sd.perm, eui, edi, euf, edf, &T.s_up, &T.s_dn, &T.e_up, &T.e_dn,
+                                &T.f_up, &T.f_dn, s));
+  ED_TRY(dev_upload((void**)&T.perm_up, su.perm.data(), su.perm.size() * 4, s));
+  ED_TRY(dev_upload((void**)&T.perm_dn, sd.perm.data(), sd.perm.size() * 4, s));
+  ED_TRY(dev_upload((void**)&T.lst_up, su.lst.data(), su.lst.size() * 4, s));
+  ED_TRY(dev_upload((void**)&T.lst_dn, sd.lst.data(), sd.lst.size() * 4, s));
+  ED_TRY(dev_upload((void**)&T.meta_up, su.meta.data(), su.meta.size() * 2, s));
+  ED_TRY(dev_upload((void**)&T.meta_dn, sd.meta.data(), sd.meta.size() * 2, s));
+  ED_CUDA(cudaStreamSynchronize(s));
+  T.pmax_up = su.pmax;
+  T.pmax_dn = sd.pmax;
+  // L2 policies (bit set = evict_last): pass 1 X loads, pass 1 S stores, pass 2 X loads, pass 2
+  // W stores
+  const char* pe = getenv("CMPY_ED_STRIPE_POL");
+  T.pol = pe ? atoi(pe) : 0b1010;
+  T.on = 1;
+  return ED_OK;
+}
+
+static void free_stripe(StripeTables& T) {
+  cudaFree(T.perm_up); cudaFree(T.perm_dn); cudaFree(T.lst_up); cudaFree(T.lst_dn);
+  cudaFree(T.meta_up); cudaFree(T.meta_dn); cudaFree(T.s_up); cudaFree(T.s_dn);
+  cudaFree(T.e_up); cudaFree(T.e_dn); cudaFree(T.f_up); cudaFree(T.f_dn);
+  T = StripeTables();
+}
+
 // Tables of the banded two-pass matvec (ed_sweep.cuh); leaves B.sw.on = 0 when the sector does
 // not suit it (odd num_dn: the 16-byte row-piece copies of pass 1 need even rows; a target with more than
 // 15 hops; a band wider than the shared memory). CMPY_ED_SWEEP=0 disables it.
@@ -1154,41 +1248,15 @@ static ed_status build_sweep(ed_plan_s* p, BfpTables& B, const std::vector<int32
   if (ru < su.need || rd < sd.need || ru == 0 || rd == 0) return ED_OK;
   sweep_lists(nu, uoff, uidx, ucoef, ru, &su);
   sweep_lists(nd, doff, didx, dcoef, rd, &sd);
-  // renumbered diagonal data
-  std::vector<uint64_t> st_up(nu), st_dn(nd), sup(nu), sdn(nd);
-  ED_CUDA(cudaMemcpyAsync(st_up.data(), p->up.states, nu * 8, cudaMemcpyDeviceToHost, s));
-  ED_CUDA(cudaMemcpyAsync(st_dn.data(), p->dn.states, nd * 8, cudaMemcpyDeviceToHost, s));
-  ED_CUDA(cudaStreamSynchronize(s));
-  for (int64_t i = 0; i < nu; ++i) sup[i] = st_up[su.perm[i]];
-  for (int64_t i = 0; i < nd; ++i) sdn[i] = st_dn[sd.perm[i]];
-  auto up = [&](auto** dst, const void* src, size_t bytes) -> ed_status {
-    ED_CUDA(cudaMalloc((void**)dst, std::max<size_t>(bytes, 8)));
-    if (bytes) ED_CUDA(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, s));
-    return ED_OK;
-  };
-  if (!B.diag64) {
-    std::vector<int32_t> a(nu), b(nd);
-    for (int64_t i = 0; i < nu; ++i) a[i] = eui[su.perm[i]];
-    for (int64_t i = 0; i < nd; ++i) b[i] = edi[sd.perm[i]];
-    ED_TRY(up(&W.e_up, a.data(), a.size() * 4));
-    ED_TRY(up(&W.e_dn, b.data(), b.size() * 4));
-    ED_CUDA(cudaStreamSynchronize(s));
-  } else {
-    std::vector<int64_t> a(nu), b(nd);
-    for (int64_t i = 0; i < nu; ++i) a[i] = euf[su.perm[i]];
-    for (int64_t i = 0; i < nd; ++i) b[i] = edf[sd.perm[i]];
-    ED_TRY(up(&W.f_up, a.data(), a.size() * 8));
-    ED_TRY(up(&W.f_dn, b.data(), b.size() * 8));
-    ED_CUDA(cudaStreamSynchronize(s));
-  }
+  ED_TRY(upload_renumbered_diag(p, B, su.perm, sd.perm, eui, edi, euf, edf, &W.s_up, &W.s_dn, &W.e_up, &W.e_dn,
+                                &W.f_up, &W.f_dn, s));
+  auto up = [&](auto** dst, const void* src, size_t bytes) { return dev_upload((void**)dst, src, bytes, s); };
   ED_TRY(up(&W.perm_up, su.perm.data(), su.perm.size() * 4));
   ED_TRY(up(&W.perm_dn, sd.perm.data(), sd.perm.size() * 4));
   ED_TRY(up(&W.lst_up, su.lst.data(), su.lst.size() * 2));
   ED_TRY(up(&W.lst_dn, sd.lst.data(), sd.lst.size() * 2));
   ED_TRY(up(&W.win_up, su.win.data(), su.win.size() * sizeof(int2)));
   ED_TRY(up(&W.win_dn, sd.win.data(), sd.win.size() * sizeof(int2)));
-  ED_TRY(up(&W.s_up, sup.data(), sup.size() * 8));
-  ED_TRY(up(&W.s_dn, sdn.data(), sdn.size() * 8));
   ED_CUDA(cudaStreamSynchronize(s));
   W.ring_up = ru;
   W.ring_dn = rd;
@@ -1415,6 +1483,7 @@ ed_status build_bfp(ed_plan_s* p, cudaStream_t s) {
   }
   ED_CUDA(cudaStreamSynchronize(s));
   ED_TRY(build_sweep(p, B, uoff, uidx, ucoef, doff, didx, dcoef, eui, edi, euf, edf, s));
+  ED_TRY(build_stripe(p, B, uoff, uidx, ucoef, doff, didx, dcoef, eui, edi, euf, edf, s));
   B.eligible = 1;
   return ED_OK;
 }
@@ -1425,6 +1494,7 @@ void free_bfp(ed_plan_s* p) {
   cudaFree(B.up_lst); cudaFree(B.up_cnt);
   cudaFree(B.e_up_int); cudaFree(B.e_dn_int); cudaFree(B.e_up_fx); cudaFree(B.e_dn_fx);
   free_sweep(B.sw);
+  free_stripe(B.sp);
   B = BfpTables();
 }
 
@@ -1471,11 +1541,12 @@ static int v3_threads(const ed_plan_s* p) {
   return (int)std::min<int64_t>(MV3_MAXNT, 32 * std::max<int64_t>(1, warps));
 }
 
-// matvec variant: 5 (banded two-pass sweep in the renumbered basis, ed_sweep.cuh) when the
-// plan has its tables, else 3 (bulk-copied double-buffered rows, bond-major dn table) when both
-// stages and the table fit in shared memory, else 2 (resident slot table, one stage), else 1.
-// Rows must have an even length (16-byte row copies). CMPY_ED_MATVEC=1|2|3|4|5 forces a
-// variant when possible.
+// matvec variant: 3 (bulk-copied double-buffered rows, bond-major dn table) when both stages
+// and the table fit in shared memory, else 5 (banded two-pass sweep in a renumbered basis,
+// ed_sweep.cuh) when the plan has its tables, else 2 (resident slot table, one stage), else 1;
+// 6 (two-pass stripes in a renumbered basis, ed_stripe.cuh) and 5 when forced. Rows must have
+// an even length (16-byte row copies). CMPY_ED_MATVEC=1..6 or ed_plan_set_matvec_variant
+// forces a variant when possible.
 static int matvec_variant(const ed_plan_s* p) {
   static int env_forced = -1;
   if (env_forced < 0) {
@@ -1493,6 +1564,7 @@ static int matvec_variant(const ed_plan_s* p) {
   // two-pass (4): column panels of 4 (nd % 4 == 0), a panel of all rows in half the shared memory
   const bool v4_ok = v3_ok && p->num_dn % MV_PW == 0 && (size_t)p->num_up * MV_PW * 8 + 1024 <= optin / 2;
   const bool v5_ok = p->bfp.sw.on != 0;
+  const bool v6_ok = p->bfp.sp.on != 0;
   if (forced == 1) return 1;
   if (forced == 2) return v2_ok ? 2 : 1;
   if (forced == 3 && v3_ok) return 3;
@@ -1501,13 +1573,35 @@ static int matvec_variant(const ed_plan_s* p) {
   // 14-site sectors it measured 0.75 ms per H*v against 0.19 ms for 3 (its pass walks one
   // stripe per CTA through the band and waits on every chunk)
   if (v5_ok && forced == 5) return 5;
+  if (v6_ok && forced == 6) return 6;
   if (v3_ok) return 3;
   if (v5_ok) return 5;
   return v2_ok ? 2 : 1;
 }
 
+// CTAs of the stripe passes (persistent, as many as the SMs hold)
+static int stripe_grid(const ed_plan_s* p, int64_t nstripes, int per_sm) {
+  return (int)std::min<int64_t>(nstripes, (int64_t)p->ctx->num_sms * per_sm);
+}
+
+// the renumbering of the plan's matvec: variants 5 and 6 keep Lanczos vectors in a renumbered
+// basis (pu, pd: new -> old); false for the variants that work in the sector's own order
+static bool matvec_perms(const ed_plan_s* p, const int32_t** pu, const int32_t** pd) {
+  const int v = matvec_variant(p);
+  *pu = *pd = nullptr;
+  if (v == 5) {
+    *pu = p->bfp.sw.perm_up;
+    *pd = p->bfp.sw.perm_dn;
+  } else if (v == 6) {
+    *pu = p->bfp.sp.perm_up;
+    *pd = p->bfp.sp.perm_dn;
+  }
+  return *pu != nullptr;
+}
+
 static int bfp_matvec_grid(const ed_plan_s* p) {
   if (matvec_variant(p) == 5) return (int)((p->num_up + SW_W - 1) / SW_W);  // pass 2 writes the partials
+  if (matvec_variant(p) == 6) return stripe_grid(p, (p->num_up + ST_K - 1) / ST_K, p->bfp.sp.per_sm_dn);
   if (matvec_variant(p) >= 3)
     return (int)std::min<int64_t>((p->num_up + MV3_R - 1) / MV3_R, (int64_t)p->ctx->num_sms);
   if (matvec_variant(p) == 2)
@@ -1597,6 +1691,37 @@ static ed_status launch_sweep(const ed_plan_s* p, const int64_t* X, int64_t* W, 
   return ED_OK;
 }
 
+// the two stripe passes on renumbered vectors: S = A X into W, then W = t (S + X B) + D X with
+// the Lanczos partials (and the step's scalars when fz.on)
+template <bool DIAG64>
+static ed_status launch_stripe(const ed_plan_s* p, const int64_t* X, int64_t* W, double* partial,
+                               unsigned long long* partial_max, BfpState* st, cudaStream_t s, const BfpFuse& fz) {
+  static std::atomic<uint64_t> done{0};
+  const uint64_t bit = 1ull << (p->device & 63);
+  if (!(done.load() & bit)) {
+    cudaFuncAttributes fa;
+    ED_CUDA(cudaFuncGetAttributes(&fa, k_stripe_up));
+    ED_CUDA(cudaFuncSetAttribute(k_stripe_up, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 p->ctx->smem_optin - (int)fa.sharedSizeBytes));
+    ED_CUDA(cudaFuncSetAttribute(k_stripe_up, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    ED_CUDA(cudaFuncGetAttributes(&fa, k_stripe_dn<DIAG64>));
+    ED_CUDA(cudaFuncSetAttribute(k_stripe_dn<DIAG64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 p->ctx->smem_optin - (int)fa.sharedSizeBytes));
+    ED_CUDA(cudaFuncSetAttribute(k_stripe_dn<DIAG64>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    done.fetch_or(bit);
+  }
+  const StripeTables& T = p->bfp.sp;
+  const int64_t nu = p->num_up, nd = p->num_dn;
+  const StripeArgs au{nu, nd, T.lst_up, T.meta_up, T.pol & 3};
+  k_stripe_up<<<stripe_grid(p, (nd + ST_K - 1) / ST_K, T.per_sm_up), ST_NT, stripe_smem(nu), s>>>(au, X, W, st);
+  const StripeArgs ad{nu, nd, T.lst_dn, T.meta_dn, (T.pol >> 2) & 3};
+  const StripeDiag dg{T.s_up, T.s_dn, T.e_up, T.e_dn, T.f_up, T.f_dn};
+  k_stripe_dn<DIAG64><<<stripe_grid(p, (nu + ST_K - 1) / ST_K, T.per_sm_dn), ST_NT, stripe_smem(nd), s>>>(
+      bfp_args(p), ad, dg, X, W, partial, partial_max, st, fz);
+  ED_CHECK_LAUNCH_N("stripe matvec", 2);
+  return ED_OK;
+}
+
 // opt-in to large dynamic shared memory once per (kernel variant, device)
 template <bool VEC2, bool DIAG64>
 static ed_status launch_variant(const ed_plan_s* p, size_t smem, int g, const int64_t* X, int64_t* W,
@@ -1627,14 +1752,22 @@ static ed_status launch_bfp_matvec(const ed_plan_s* p, const int64_t* X, int64_t
   // v2/v3 and the paired-column v1 move 16 bytes at a time (bulk row copies, v2 loads and
   // stores): they need 16-byte aligned X and W, always true for the Lanczos store; other
   // caller buffers take the one-column v1 kernel
+  // (the stripe matvec checks its own alignment and keeps its renumbered basis)
   const bool aligned = (((uintptr_t)X | (uintptr_t)W) & 15) == 0;
-  const int var = aligned ? matvec_variant(p) : 1;
+  const int var = (aligned || matvec_variant(p) == 6) ? matvec_variant(p) : 1;
   if (var == 5) {
     // renumbered vectors (the callers that choose variant 5 convert in and out)
     const BfpFuse& f = (fz && partial && st) ? *fz : off;
     if (fused) *fused = f.on != 0;
     return p->bfp.diag64 ? launch_sweep<true>(p, X, W, partial, partial_max, st, s, f)
                          : launch_sweep<false>(p, X, W, partial, partial_max, st, s, f);
+  }
+  if (var == 6) {
+    // renumbered vectors, as for variant 5
+    const BfpFuse& f = (fz && partial && st) ? *fz : off;
+    if (fused) *fused = f.on != 0;
+    return p->bfp.diag64 ? launch_stripe<true>(p, X, W, partial, partial_max, st, s, f)
+                         : launch_stripe<false>(p, X, W, partial, partial_max, st, s, f);
   }
   if (var >= 3) {
     const BfpFuse& f = (fz && partial && st) ? *fz : off;
@@ -1722,17 +1855,17 @@ static BfpRun bfp_bind(const ed_plan_s* p, void* work, int K, bool store) {
 }
 
 // start vector (FP64, device) -> R_0 in BFP, beta_0 = ||v0||
-// (renum: the run uses the sweep matvec, R_0 is stored in its renumbered basis)
+// (pu, pd non-null: the run's matvec works in a renumbered basis, R_0 is stored in it)
 static ed_status bfp_start(const ed_plan_s* p, BfpRun& r, const double* v0, double* beta, cudaStream_t s,
-                           bool renum) {
+                           const int32_t* pu, const int32_t* pd) {
   const int64_t D = p->dim;
   const int gs = grid_for(D, 256, p->ctx->num_sms * 8);
   unsigned long long* mxb = (unsigned long long*)(r.misc + 8);
   ED_CUDA(cudaMemsetAsync(mxb, 0, 8, s));
   k_maxabs_f64<<<gs, BT, 0, s>>>(v0, D, mxb);
-  if (renum)
-    k_f64_to_bfp_perm<<<gs, 256, 0, s>>>(v0, p->num_up, p->num_dn, p->bfp.sw.perm_up, p->bfp.sw.perm_dn, mxb,
-                                         p->bfp.m_in, r.v.vec(0), r.v.eR, r.v.maxR);
+  if (pu)
+    k_f64_to_bfp_perm<<<gs, 256, 0, s>>>(v0, p->num_up, p->num_dn, pu, pd, mxb, p->bfp.m_in, r.v.vec(0), r.v.eR,
+                                         r.v.maxR);
   else
     k_f64_to_bfp<<<gs, 256, 0, s>>>(v0, D, mxb, p->bfp.m_in, r.v.vec(0), r.v.eR, r.v.maxR);
   k_bfp_norm<<<r.L.nparts, BT, 0, s>>>(r.v, 0, r.part, r.st, beta);
@@ -1797,11 +1930,12 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
   const int64_t D = p->dim;
   const bool store = prm->want_vector != 0;
   BfpRun r = bfp_bind(p, work, K, store);
-  const bool renum = matvec_variant(p) == 5;
+  const int32_t *pu, *pd;
+  (void)matvec_perms(p, &pu, &pd);
   ED_CUDA(cudaMemsetAsync(r.st, 0, sizeof(BfpState), s));
   ED_CUDA(cudaMemsetAsync(alpha, 0, K * sizeof(double), s));
   ED_CUDA(cudaMemsetAsync(beta, 0, (K + 1) * sizeof(double), s));
-  ED_TRY(bfp_start(p, r, v0_dev, beta, s, renum));
+  ED_TRY(bfp_start(p, r, v0_dev, beta, s, pu, pd));
   const int Km = (int)std::min<int64_t>(K, D);
   std::vector<cudaEvent_t> ev;
   if (prm->profile) {
@@ -1836,8 +1970,7 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
   if (evec) {
     k_bfp_ritz_coef<<<1, BT, 0, s>>>(r.c, beta, r.v.eR, r.tri, r.C, r.misc);
     k_bfp_ritz<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(
-        r.v, r.C, r.misc, r.st, evec, renum ? p->bfp.sw.perm_up : nullptr, renum ? p->bfp.sw.perm_dn : nullptr,
-        p->num_dn);
+        r.v, r.C, r.misc, r.st, evec, pu, pd, p->num_dn);
     ED_CHECK_LAUNCH_N("k_bfp_ritz", 2);
   }
   BfpState hs;
@@ -1888,7 +2021,9 @@ ed_status bfp_lanczos_coeffs(const ed_plan_s* p, int K, const double* start, voi
     if (!std::isfinite(mx)) return fail(ED_ERR_NONFINITE, "start vector is not finite");
     if (mx == 0.0) { *steps = 0; *norm = 0.0; return ED_OK; }
   }
-  ED_TRY(bfp_start(p, r, start, beta, s, matvec_variant(p) == 5));
+  const int32_t *pu, *pd;
+  (void)matvec_perms(p, &pu, &pd);
+  ED_TRY(bfp_start(p, r, start, beta, s, pu, pd));
   const int Km = (int)std::min<int64_t>(K, D);
   for (int k = 0; k < Km; ++k) ED_TRY(bfp_step(p, r, k, alpha, beta, s));
   BfpState hs;
@@ -1960,17 +2095,19 @@ ED_API ed_status ed_matvec_fixed(ed_plan p, const int64_t* d_xm, int32_t ex, int
   if (!d_xm || !d_wm) return fail(ED_ERR_INVALID_ARG, "null vector");
   if (d_xm == d_wm) return fail(ED_ERR_INVALID_ARG, "x and w must not alias");
   cudaStream_t s = as_stream(stream);
-  if ((((uintptr_t)d_xm | (uintptr_t)d_wm) & 15) == 0 && matvec_variant(p) == 5) {
-    // the sweep matvec works in its renumbered basis: renumber x, apply, renumber back
+  const int32_t *pu, *pd;
+  if (matvec_perms(p, &pu, &pd)) {
+    // the matvec works in its renumbered basis: renumber x, apply, renumber back (through an
+    // aligned scratch buffer, whatever the alignment of the caller's vectors)
     int64_t* tmp = nullptr;
-    ED_CUDA(cudaMallocAsync((void**)&tmp, 2 * (size_t)p->dim * sizeof(int64_t), s));
+    const int64_t off = (p->dim + 1) & ~(int64_t)1;  // W 16-byte aligned like X
+    ED_CUDA(cudaMallocAsync((void**)&tmp, (size_t)(off + p->dim) * sizeof(int64_t), s));
     const int g = grid_for(p->dim, 256, p->ctx->num_sms * 8);
-    const SweepTables& w = p->bfp.sw;
-    k_sweep_permute<<<g, 256, 0, s>>>(d_xm, tmp, p->num_up, p->num_dn, w.perm_up, w.perm_dn, 1);
+    k_sweep_permute<<<g, 256, 0, s>>>(d_xm, tmp, p->num_up, p->num_dn, pu, pd, 1);
     ED_CHECK_LAUNCH("k_sweep_permute");
-    ed_status st = launch_bfp_matvec(p, tmp, tmp + p->dim, nullptr, nullptr, nullptr, s);
+    ed_status st = launch_bfp_matvec(p, tmp, tmp + off, nullptr, nullptr, nullptr, s);
     if (st == ED_OK) {
-      k_sweep_permute<<<g, 256, 0, s>>>(tmp + p->dim, d_wm, p->num_up, p->num_dn, w.perm_up, w.perm_dn, 0);
+      k_sweep_permute<<<g, 256, 0, s>>>(tmp + off, d_wm, p->num_up, p->num_dn, pu, pd, 0);
       ED_CHECK_LAUNCH("k_sweep_permute");
     }
     ED_CUDA(cudaFreeAsync(tmp, s));
@@ -1990,7 +2127,7 @@ ED_API int ed_plan_matvec_variant(ed_plan p) { return (p && p->bfp.eligible) ? m
 
 ED_API ed_status ed_plan_set_matvec_variant(ed_plan p, int variant) {
   ED_TRY(check_plan(p));
-  if (variant < 0 || variant > 5) return fail(ED_ERR_INVALID_ARG, "variant must be in [0, 5]");
+  if (variant < 0 || variant > 6) return fail(ED_ERR_INVALID_ARG, "variant must be in [0, 6]");
   p->bfp.force_var = variant;
   return ED_OK;
 }

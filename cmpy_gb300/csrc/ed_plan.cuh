@@ -37,6 +37,29 @@ struct FermionParams {
 // dn states are renumbered (reverse Cuthill-McKee order of each spin's hop graph) so that the
 // single-spin hop matrices are banded; a Lanczos run that uses this matvec keeps its vectors
 // in the renumbered basis (index u' * num_dn + d').
+// tables of the stripe matvec (variant 6, ed_stripe.cuh): states renumbered by hop count, hop
+// lists in list-major pairs of 16-bit record slots
+struct StripeTables {
+  int on = 0;
+  int per_sm_up = 0, per_sm_dn = 0;  // CTAs per SM of pass 1 / pass 2 (shared memory)
+  int pmax_up = 0, pmax_dn = 0;      // list pairs per target, largest
+  int32_t* perm_up = nullptr;        // [nu] renumbered -> original up index
+  int32_t* perm_dn = nullptr;        // [nd]
+  // per renumbered target: pairs of partner record slots (+ pairs first, then - pairs, each
+  // segment padded to whole pairs with the zero record), list-major [pair][n] uint32
+  uint32_t* lst_up = nullptr;
+  uint32_t* lst_dn = nullptr;
+  uint16_t* meta_up = nullptr;       // [nu]: + pairs | - pairs << 8
+  uint16_t* meta_dn = nullptr;       // [nd]
+  uint64_t* s_up = nullptr;          // states, renumbered
+  uint64_t* s_dn = nullptr;
+  int32_t* e_up = nullptr;           // diagonal mode 0 energies, renumbered
+  int32_t* e_dn = nullptr;
+  int64_t* f_up = nullptr;           // diagonal mode 1 energies, renumbered
+  int64_t* f_dn = nullptr;
+  int pol = 0;                       // L2 policy selection (see ed_stripe.cuh)
+};
+
 struct SweepTables {
   int on = 0;
   int ring_up = 0, ring_dn = 0;  // ring capacity in chunks of 32 rows (pass 1) / 32 columns (pass 2)
@@ -104,6 +127,7 @@ struct BfpTables {
   int32_t* e_up_int = nullptr;  // [nu]
   int32_t* e_dn_int = nullptr;  // [nd]
   SweepTables sw;
+  StripeTables sp;
   long wait_limit = 0;          // polls of a first bulk-copy wait before giving up (0: default)
   int force_var = 0;            // matvec variant chosen for this plan (0: automatic)
 };
