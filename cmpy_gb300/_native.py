@@ -144,6 +144,8 @@ _SIGNATURES = {
     "ed_tridiag_lowest_noalloc": (I32, [P, P, I32, P, P, P]),
     "ed_tridiag_lowest_batch": (I32, [P, I32, P, I32, P, I32, I32, P, P, I32, P]),
     "ed_tridiag_pinv_solve_batch": (I32, [P, I32, P, I32, P, I32, I32, P, P, I32, P, P, I32, P]),
+    "ed_dense_eigh_batch": (I32, [P, I64, I64, P, I32, I32, P, P, I64, I64, P]),
+    "ed_tridiag_eigh": (I32, [P, P, I32, P, P, I64, P]),
     "ed_batch_create": (I32, [C.POINTER(C.c_void_p), I32, C.POINTER(C.c_void_p)]),
     "ed_batch_destroy": (I32, [C.c_void_p]),
     "ed_batch_workspace": (I32, [C.c_void_p, I32, I32, I32, I32, C.POINTER(C.c_size_t)]),

@@ -1,0 +1,408 @@
+// Dense symmetric eigensolver for batches of sector matrices, FP64 — the device replacement of
+// numpy.linalg.eigh in cmpy/exactdiag.py:46-57 (solve_sector: every eigenpair of a sector's
+// dense Hamiltonian) and the dense branch of exactdiag.py:24-43.
+//
+// For every matrix of the batch (order n_b <= n_max, row-major, overwritten):
+// 1. Householder tridiagonalisation A = Q T Q^T. Step k takes the reflector of row k beyond
+//    the diagonal, p = tau A22 v, w = p - (tau/2)(p.v) v, A22 -= v w^T + w v^T. Each step is
+//    four launches over the whole batch (reflector, matrix-vector product with one warp per row,
+//    the dot product, rank-2 update), so a single large matrix uses every SM; the FP64 pipe of
+//    this GPU (two FMAs per clock per SM) bounds the O(n^3) parts. The rank-2 update is formed
+//    as v_i w_j + w_i v_j with separately rounded products, so A stays exactly symmetric.
+// 2. All eigenvalues of T by bisection on Sturm counts (one thread per eigenvalue), ascending.
+// 3. Eigenvectors of T by inverse iteration (Gaussian elimination with partial pivoting of
+//    T - lambda I, start vectors that differ per index), one thread per cluster of eigenvalues
+//    closer than 1e-7 max(1, |lambda|max): each iterate is re-orthogonalised against the
+//    cluster's earlier members, so degenerate sector eigenvalues (symmetries) give an
+//    orthonormal basis of the eigenspace.
+// 4. Back-transformation y = Q z (one warp per eigenvector, reflectors in reverse order).
+// Output: eigenvalues ascending, eigenvector i as row i of Z (Z = V^T).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ed_common.cuh"
+#include "ed_tridiag.cuh"
+
+namespace ed {
+
+constexpr int DE_NT = 256;
+
+struct DenseBatch {
+  double* A;          // [B] matrices, row-major
+  int64_t lda, sa;    // leading dimension, matrix stride
+  const int* n;       // [B] orders
+  double* d;          // [B][nmax] diagonal of T
+  double* bet;        // [B][nmax] bet[i] couples i-1 and i (bet[0] = 0)
+  double* tau;        // [B][nmax] reflector scales
+  double* P;          // [B][nmax] p, then w
+  double* glim;       // [B][2] Gershgorin bounds of T
+  int nmax;
+};
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// step k, one CTA per matrix: the reflector of row k (A[k][k+1..n)), kept in that row with its
+// first element replaced by x0 - alpha; tau[k]; d[k] = A[k][k]; bet[k+1] = alpha
+__global__ void __launch_bounds__(DE_NT) k_hh_column(DenseBatch m, int k) {
+  __shared__ double sm[DE_NT / 32];
+  const int b = blockIdx.x, n = m.n[b];
+  if (k > n - 3) return;
+  double* row = m.A + (size_t)b * m.sa + (size_t)k * m.lda;
+  double s = 0.0;
+  for (int i = k + 2 + threadIdx.x; i < n; i += DE_NT) s = fma(row[i], row[i], s);
+  s = block_sum<DE_NT>(s, sm);
+  if (threadIdx.x == 0) {
+    const double x0 = row[k + 1];
+    double t = 0.0, alpha = x0;
+    if (s > 0.0) {
+      const double nrm = sqrt(fma(x0, x0, s));
+      alpha = x0 >= 0.0 ? -nrm : nrm;
+      const double v0 = x0 - alpha;
+      t = 2.0 / fma(v0, v0, s);
+      row[k + 1] = v0;
+    }
+    m.tau[(size_t)b * m.nmax + k] = t;
+    m.d[(size_t)b * m.nmax + k] = row[k];
+    m.bet[(size_t)b * m.nmax + k + 1] = alpha;
+  }
+}
+
+// step k: p_i = tau sum_{j>k} A[i][j] v_j for i > k (one warp per row)
+__global__ void __launch_bounds__(DE_NT) k_hh_matvec(DenseBatch m, int k) {
+  const int b = blockIdx.y, n = m.n[b];
+  if (k > n - 3) return;
+  const int i = k + 1 + blockIdx.x * (DE_NT / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const double t = m.tau[(size_t)b * m.nmax + k];
+  const double* Ab = m.A + (size_t)b * m.sa;
+  const double* v = Ab + (size_t)k * m.lda;
+  const double* ai = Ab + (size_t)i * m.lda;
+  double s = 0.0;
+  for (int j = k + 1 + lane; j < n; j += 32) s = fma(ai[j], v[j], s);
+  s = warp_sum_d(s);
+  if (lane == 0) m.P[(size_t)b * m.nmax + i] = t * s;
+}
+
+// step k, one CTA per matrix: w = p - (tau/2)(p.v) v in place of p
+__global__ void __launch_bounds__(DE_NT) k_hh_dot(DenseBatch m, int k) {
+  __shared__ double sm[DE_NT / 32];
+  __shared__ double kk;
+  const int b = blockIdx.x, n = m.n[b];
+  if (k > n - 3) return;
+  const double* v = m.A + (size_t)b * m.sa + (size_t)k * m.lda;
+  double* p = m.P + (size_t)b * m.nmax;
+  double s = 0.0;
+  for (int i = k + 1 + threadIdx.x; i < n; i += DE_NT) s = fma(p[i], v[i], s);
+  s = block_sum<DE_NT>(s, sm);
+  if (threadIdx.x == 0) kk = 0.5 * m.tau[(size_t)b * m.nmax + k] * s;
+  __syncthreads();
+  for (int i = k + 1 + threadIdx.x; i < n; i += DE_NT) p[i] = fma(-kk, v[i], p[i]);
+}
+
+// step k: A[i][j] -= v_i w_j + w_i v_j for i, j > k (products rounded separately: symmetric)
+__global__ void __launch_bounds__(DE_NT) k_hh_update(DenseBatch m, int k) {
+  const int b = blockIdx.y, n = m.n[b];
+  if (k > n - 3) return;
+  const int i = k + 1 + blockIdx.x;
+  if (i >= n) return;
+  if (m.tau[(size_t)b * m.nmax + k] == 0.0) return;
+  double* Ab = m.A + (size_t)b * m.sa;
+  const double* v = Ab + (size_t)k * m.lda;
+  const double* w = m.P + (size_t)b * m.nmax;
+  const double vi = v[i], wi = w[i];
+  double* ai = Ab + (size_t)i * m.lda;
+  for (int j = k + 1 + threadIdx.x; j < n; j += DE_NT)
+    ai[j] = __dsub_rn(ai[j], __dadd_rn(__dmul_rn(vi, w[j]), __dmul_rn(wi, v[j])));
+}
+
+// the last diagonal entries and the Gershgorin bounds of T (one thread per matrix)
+__global__ void k_hh_finish(DenseBatch m, int B) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int n = m.n[b];
+  const double* Ab = m.A + (size_t)b * m.sa;
+  double* d = m.d + (size_t)b * m.nmax;
+  double* bt = m.bet + (size_t)b * m.nmax;
+  bt[0] = 0.0;
+  if (n >= 2) {
+    d[n - 2] = Ab[(size_t)(n - 2) * m.lda + n - 2];
+    bt[n - 1] = Ab[(size_t)(n - 2) * m.lda + n - 1];
+  }
+  d[n - 1] = Ab[(size_t)(n - 1) * m.lda + n - 1];
+  double lo = d[0], hi = d[0];
+  for (int i = 0; i < n; ++i) {
+    const double r = (i > 0 ? fabs(bt[i]) : 0.0) + (i + 1 < n ? fabs(bt[i + 1]) : 0.0);
+    lo = fmin(lo, d[i] - r);
+    hi = fmax(hi, d[i] + r);
+  }
+  const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
+  m.glim[2 * b] = lo - pad;
+  m.glim[2 * b + 1] = hi + pad;
+}
+
+// a given tridiagonal (alpha[0..m), beta[1..m)) as T of a one-matrix batch, and its Gershgorin
+// bounds (one thread)
+__global__ void k_tri_setup(DenseBatch m, const double* alpha, const double* beta, int n) {
+  for (int i = 0; i < n; ++i) {
+    m.d[i] = alpha[i];
+    m.bet[i] = i > 0 ? beta[i] : 0.0;
+  }
+  double lo = m.d[0], hi = m.d[0];
+  for (int i = 0; i < n; ++i) {
+    const double r = (i > 0 ? fabs(m.bet[i]) : 0.0) + (i + 1 < n ? fabs(m.bet[i + 1]) : 0.0);
+    lo = fmin(lo, m.d[i] - r);
+    hi = fmax(hi, m.d[i] + r);
+  }
+  const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
+  m.glim[0] = lo - pad;
+  m.glim[1] = hi + pad;
+}
+
+// eigenvalue i of T by bisection: the smallest x with at least i + 1 eigenvalues below
+__global__ void k_tri_eigvals(DenseBatch m, int B, double* W) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int b = (int)(g / m.nmax), i = (int)(g % m.nmax);
+  if (b >= B) return;
+  const int n = m.n[b];
+  if (i >= n) return;
+  const double* d = m.d + (size_t)b * m.nmax;
+  const double* bt = m.bet + (size_t)b * m.nmax;
+  double lo = m.glim[2 * b], hi = m.glim[2 * b + 1];
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (sturm_count(d, bt, nullptr, n, mid) >= i + 1) hi = mid;
+    else lo = mid;
+  }
+  W[(size_t)b * m.nmax + i] = 0.5 * (lo + hi);
+}
+
+// The eigenvectors of T by inverse iteration, one thread per cluster of eigenvalues (values
+// closer than ctol = 1e-7 max(1, |lambda|max) to their neighbour; most clusters are single
+// values). Each member: Gaussian elimination with partial pivoting of T - lambda I (pivots
+// kept as reciprocals), three solves from a start vector that differs with the index, each
+// followed by modified Gram-Schmidt against the cluster's earlier members, so that the
+// members of a degenerate eigenvalue converge to an orthonormal basis of its eigenspace.
+// work: 5 n doubles of the thread.
+__global__ void k_tri_eigvecs(DenseBatch m, int B, const double* W, double* Z, int64_t ldz, int64_t sz,
+                              double* work) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int b = (int)(g / m.nmax), i0 = (int)(g % m.nmax);
+  if (b >= B) return;
+  const int n = m.n[b];
+  if (i0 >= n) return;
+  const double* w = W + (size_t)b * m.nmax;
+  const double ctol = 1e-7 * fmax(1.0, fmax(fabs(w[0]), fabs(w[n - 1])));
+  if (i0 > 0 && w[i0] - w[i0 - 1] <= ctol) return;  // not the first member of its cluster
+  int i1 = i0 + 1;
+  while (i1 < n && w[i1] - w[i1 - 1] <= ctol) ++i1;
+  const double* a = m.d + (size_t)b * m.nmax;
+  const double* bt = m.bet + (size_t)b * m.nmax;
+  double* Zb = Z + (size_t)b * sz;
+  double* wk = work + ((size_t)b * m.nmax + i0) * 5 * (size_t)m.nmax;
+  double* dd = wk;
+  double* du = wk + n;
+  double* du2 = wk + 2 * n;
+  double* ml = wk + 3 * n;
+  double* pv = wk + 4 * n;
+  for (int q = i0; q < i1; ++q) {
+    const double ev = w[q];
+    double* vec = Zb + (size_t)q * ldz;
+    const double tiny = 1e-300 + 1e-18 * fmax(fabs(ev), 1.0);
+    uint32_t h = 2654435761u * (uint32_t)(q + 1);
+    for (int r = 0; r < n; ++r) {
+      h ^= h << 13;
+      h ^= h >> 17;
+      h ^= h << 5;
+      vec[r] = 0.5 + (double)(h & 0xffffu) / 65536.0;
+    }
+    for (int r = 0; r < n; ++r) {
+      dd[r] = a[r] - ev;
+      du[r] = (r + 1 < n) ? bt[r + 1] : 0.0;
+      du2[r] = 0.0;
+    }
+    for (int r = 0; r < n - 1; ++r) {
+      const double sub = bt[r + 1];
+      if (fabs(dd[r]) >= fabs(sub)) {
+        pv[r] = 0.0;
+        if (dd[r] == 0.0) dd[r] = tiny;
+        const double rc = 1.0 / dd[r];
+        const double l = sub * rc;
+        ml[r] = l;
+        dd[r + 1] -= l * du[r];
+        dd[r] = rc;
+      } else {
+        pv[r] = 1.0;
+        const double rc = 1.0 / sub;
+        const double l = dd[r] * rc;
+        ml[r] = l;
+        const double t0 = dd[r + 1], t1 = (r + 2 < n) ? du[r + 1] : 0.0, odu = du[r];
+        du[r] = t0;
+        du2[r] = t1;
+        dd[r + 1] = odu - l * t0;
+        if (r + 2 < n) du[r + 1] = -l * t1;
+        dd[r] = rc;
+      }
+    }
+    if (dd[n - 1] == 0.0) dd[n - 1] = tiny;
+    dd[n - 1] = 1.0 / dd[n - 1];
+    for (int it = 0; it < 3; ++it) {
+      for (int r = 0; r < n - 1; ++r) {
+        if (pv[r] != 0.0) {
+          const double t = vec[r];
+          vec[r] = vec[r + 1];
+          vec[r + 1] = t - ml[r] * vec[r];
+        } else {
+          vec[r + 1] -= ml[r] * vec[r];
+        }
+      }
+      for (int r = n - 1; r >= 0; --r) {
+        double sacc = vec[r];
+        if (r + 1 < n) sacc -= du[r] * vec[r + 1];
+        if (r + 2 < n) sacc -= du2[r] * vec[r + 2];
+        vec[r] = sacc * dd[r];
+      }
+      double mx = 0.0;
+      for (int r = 0; r < n; ++r) mx = fmax(mx, fabs(vec[r]));
+      const double sc = mx > 0.0 ? 1.0 / mx : 1.0;  // keep the iterate in range
+      for (int r = 0; r < n; ++r) vec[r] *= sc;
+      for (int pass = 0; pass < 2; ++pass)
+        for (int l = i0; l < q; ++l) {
+          const double* zl = Zb + (size_t)l * ldz;
+          double sp = 0.0;
+          for (int r = 0; r < n; ++r) sp = fma(zl[r], vec[r], sp);
+          for (int r = 0; r < n; ++r) vec[r] = fma(-sp, zl[r], vec[r]);
+        }
+      double nrm = 0.0;
+      for (int r = 0; r < n; ++r) nrm = fma(vec[r], vec[r], nrm);
+      nrm = 1.0 / sqrt(nrm);
+      for (int r = 0; r < n; ++r) vec[r] *= nrm;
+    }
+  }
+}
+
+// y = Q z for every eigenvector (one warp per vector): reflectors n-3 .. 0
+__global__ void __launch_bounds__(DE_NT) k_hh_back(DenseBatch m, int B, double* Z, int64_t ldz, int64_t sz) {
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int b = (int)(gw / m.nmax), i = (int)(gw % m.nmax);
+  if (b >= B) return;
+  const int n = m.n[b];
+  if (i >= n) return;
+  const double* Ab = m.A + (size_t)b * m.sa;
+  double* y = Z + (size_t)b * sz + (size_t)i * ldz;
+  for (int k = n - 3; k >= 0; --k) {
+    const double t = m.tau[(size_t)b * m.nmax + k];
+    if (t == 0.0) continue;
+    const double* v = Ab + (size_t)k * m.lda;
+    double s = 0.0;
+    for (int j = k + 1 + lane; j < n; j += 32) s = fma(v[j], y[j], s);
+    s = t * warp_sum_d(s);
+    for (int j = k + 1 + lane; j < n; j += 32) y[j] = fma(-s, v[j], y[j]);
+    __syncwarp();
+  }
+}
+
+}  // namespace ed
+
+using namespace ed;
+
+extern "C" {
+
+ED_API ed_status ed_dense_eigh_batch(double* d_a, int64_t lda, int64_t stride_a, const int* h_n, int B, int n_max,
+                                     double* d_w, double* d_z, int64_t ldz, int64_t stride_z, ed_stream_t stream) {
+  if (B < 1 || n_max < 1) return fail(ED_ERR_INVALID_ARG, "B and n_max must be >= 1");
+  if (!d_a || !h_n || !d_w || !d_z) return fail(ED_ERR_INVALID_ARG, "null pointer");
+  if (lda < n_max || stride_a < (int64_t)n_max * lda || ldz < n_max || stride_z < (int64_t)n_max * ldz)
+    return fail(ED_ERR_INVALID_ARG, "leading dimensions or strides smaller than n_max");
+  for (int b = 0; b < B; ++b)
+    if (h_n[b] < 1 || h_n[b] > n_max) return fail(ED_ERR_INVALID_ARG, "matrix order outside [1, n_max]");
+  DeviceContext* ctx;
+  ED_TRY(device_context(&ctx));
+  cudaStream_t s = as_stream(stream);
+  const size_t nm = (size_t)B * n_max;
+  double* buf = nullptr;
+  int* dn = nullptr;
+  // d, bet, tau, P (4 nm), Gershgorin (2 B), inverse-iteration work (5 nm n_max)
+  ED_CUDA(cudaMallocAsync((void**)&buf, (4 * nm + 2 * (size_t)B + 5 * nm * (size_t)n_max) * sizeof(double), s));
+  ED_CUDA(cudaMallocAsync((void**)&dn, (size_t)B * sizeof(int), s));
+  ED_CUDA(cudaMemcpyAsync(dn, h_n, (size_t)B * sizeof(int), cudaMemcpyHostToDevice, s));
+  DenseBatch m;
+  m.A = d_a;
+  m.lda = lda;
+  m.sa = stride_a;
+  m.n = dn;
+  m.d = buf;
+  m.bet = buf + nm;
+  m.tau = buf + 2 * nm;
+  m.P = buf + 3 * nm;
+  m.glim = buf + 4 * nm;
+  m.nmax = n_max;
+  double* work = buf + 4 * nm + 2 * (size_t)B;
+  ed_status st = ED_OK;
+  const int rows_per = DE_NT / 32;
+  for (int k = 0; k + 3 <= n_max && st == ED_OK; ++k) {
+    const int rem = n_max - k - 1;
+    k_hh_column<<<B, DE_NT, 0, s>>>(m, k);
+    k_hh_matvec<<<dim3((rem + rows_per - 1) / rows_per, B), DE_NT, 0, s>>>(m, k);
+    k_hh_dot<<<B, DE_NT, 0, s>>>(m, k);
+    k_hh_update<<<dim3(rem, B), DE_NT, 0, s>>>(m, k);
+    const cudaError_t e = cudaGetLastError();
+    count_launches(4);
+    if (e != cudaSuccess) st = cuda_fail(e, "Householder step");
+  }
+  if (st == ED_OK) {
+    k_hh_finish<<<(B + 127) / 128, 128, 0, s>>>(m, B);
+    const int64_t nt = (int64_t)B * n_max;
+    const int g1 = (int)((nt + 127) / 128);
+    k_tri_eigvals<<<g1, 128, 0, s>>>(m, B, d_w);
+    k_tri_eigvecs<<<g1, 128, 0, s>>>(m, B, d_w, d_z, ldz, stride_z, work);
+    k_hh_back<<<(int)((nt * 32 + DE_NT - 1) / DE_NT), DE_NT, 0, s>>>(m, B, d_z, ldz, stride_z);
+    const cudaError_t e = cudaGetLastError();
+    count_launches(4);
+    if (e != cudaSuccess) st = cuda_fail(e, "tridiagonal eigenpairs");
+  }
+  cudaFreeAsync(buf, s);
+  cudaFreeAsync(dn, s);
+  return st;
+}
+
+ED_API ed_status ed_tridiag_eigh(const double* d_alpha, const double* d_beta, int m, double* d_w, double* d_z,
+                                 int64_t ldz, ed_stream_t stream) {
+  if (m < 1) return fail(ED_ERR_INVALID_ARG, "m must be >= 1");
+  if (!d_alpha || !d_beta || !d_w || !d_z) return fail(ED_ERR_INVALID_ARG, "null pointer");
+  if (ldz < m) return fail(ED_ERR_INVALID_ARG, "ldz smaller than m");
+  DeviceContext* ctx;
+  ED_TRY(device_context(&ctx));
+  cudaStream_t s = as_stream(stream);
+  double* buf = nullptr;
+  int* dn = nullptr;
+  ED_CUDA(cudaMallocAsync((void**)&buf, (4 * (size_t)m + 2 + 5 * (size_t)m * m) * sizeof(double), s));
+  ED_CUDA(cudaMallocAsync((void**)&dn, sizeof(int), s));
+  ED_CUDA(cudaMemcpyAsync(dn, &m, sizeof(int), cudaMemcpyHostToDevice, s));
+  DenseBatch b{};
+  b.n = dn;
+  b.d = buf;
+  b.bet = buf + m;
+  b.tau = buf + 2 * (size_t)m;
+  b.P = buf + 3 * (size_t)m;
+  b.glim = buf + 4 * (size_t)m;
+  b.nmax = m;
+  const int g1 = (m + 127) / 128;
+  k_tri_setup<<<1, 1, 0, s>>>(b, d_alpha, d_beta, m);
+  k_tri_eigvals<<<g1, 128, 0, s>>>(b, 1, d_w);
+  k_tri_eigvecs<<<g1, 128, 0, s>>>(b, 1, d_w, d_z, ldz, (int64_t)m * ldz, buf + 4 * (size_t)m + 2);
+  const cudaError_t e = cudaGetLastError();
+  count_launches(3);
+  cudaFreeAsync(buf, s);
+  cudaFreeAsync(dn, s);
+  if (e != cudaSuccess) return cuda_fail(e, "tridiagonal eigenpairs");
+  return ED_OK;
+}
+
+}  // extern "C"

@@ -73,6 +73,14 @@ __device__ __forceinline__ void stripe_hops(const unsigned char* sm, const Strip
   r[3] = a3 - b3;
 }
 
+// a load of S that the compiler must not move out of its condition (S may end at the last
+// row, and lanes past the last column would read beyond it)
+__device__ __forceinline__ int64_t stripe_ld_s(const int64_t* p, uint64_t pol) {
+  int64_t v;
+  asm volatile("ld.global.nc.L2::cache_hint.s64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol));
+  return v;
+}
+
 // element j of record i
 __device__ __forceinline__ int64_t* stripe_elem(unsigned char* sm, int64_t i, int j) {
   return (int64_t*)(sm + ((stripe_slot(i) ^ (uint32_t)(j >> 1)) << 4) + ((j & 1) << 3));
@@ -177,7 +185,7 @@ __global__ void __launch_bounds__(ST_NT, 2)
       // S of the four rows (written by pass 1), requested first
       int64_t sv[ST_K];
 #pragma unroll
-      for (int j = 0; j < ST_K; ++j) sv[j] = (valid && j < nrows) ? ld_keep(W + (u0 + j) * nd + d, pol_s) : 0;
+      for (int j = 0; j < ST_K; ++j) sv[j] = (valid && j < nrows) ? stripe_ld_s(W + (u0 + j) * nd + d, pol_s) : 0;
       const uint64_t sd = valid ? __ldg(dg.s_dn + d) : 0;
       const int64_t ed = !valid ? 0 : (DIAG64 ? __ldg(dg.f_dn + d) : (int64_t)__ldg(dg.e_dn + d));
       int64_t r[ST_K];

@@ -497,6 +497,47 @@ def tridiag_lowest_batch(alpha: torch.Tensor, beta: torch.Tensor, m) -> tuple[to
     return vals, vecs
 
 
+def dense_eigh_batch(mats) -> list[tuple[torch.Tensor, torch.Tensor]]:
+    """Every eigenpair of each real symmetric matrix in `mats` (square tensors), one call for
+    the batch: [(eigenvalues ascending [n], eigenvectors as columns [n, n])] on the device.
+    The hand-written FP64 solver (Householder, Sturm bisection, inverse iteration)."""
+    ms = [_as_dev_f64(a) for a in mats]
+    if not ms:
+        return []
+    sizes = [int(a.shape[0]) for a in ms]
+    if any(a.dim() != 2 or a.shape[0] != a.shape[1] or a.shape[0] < 1 for a in ms):
+        raise ValueError("dense_eigh_batch takes non-empty square matrices")
+    B, nmax = len(ms), max(sizes)
+    A = torch.zeros((B, nmax, nmax), dtype=torch.float64, device=device())
+    for b, a in enumerate(ms):
+        A[b, : sizes[b], : sizes[b]] = a
+    W = torch.empty((B, nmax), dtype=torch.float64, device=device())
+    Z = torch.zeros((B, nmax, nmax), dtype=torch.float64, device=device())
+    hn = (C.c_int * B)(*sizes)
+    N.check(N.lib().ed_dense_eigh_batch(N.ptr(A), nmax, nmax * nmax, hn, B, nmax, N.ptr(W), N.ptr(Z), nmax,
+                                        nmax * nmax, _stream()))
+    return [(W[b, : sizes[b]], Z[b, : sizes[b], : sizes[b]].t()) for b in range(B)]
+
+
+def dense_eigh(a: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
+    """(eigenvalues ascending, eigenvectors as columns) of one real symmetric matrix."""
+    return dense_eigh_batch([a])[0]
+
+
+def tridiag_eigh(alpha: torch.Tensor, beta: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
+    """Every eigenpair of the tridiagonal (alpha[0..m), beta[1..m)): (eigenvalues ascending,
+    eigenvectors as columns [m, m]) on the device."""
+    a = _as_dev_f64(alpha).contiguous().reshape(-1)
+    b = _as_dev_f64(beta).contiguous().reshape(-1)
+    m = a.numel()
+    if b.numel() < m:
+        raise ValueError("beta needs m entries (beta[0] unused)")
+    w = torch.empty(m, dtype=torch.float64, device=device())
+    z = torch.zeros((m, m), dtype=torch.float64, device=device())
+    N.check(N.lib().ed_tridiag_eigh(N.ptr(a), N.ptr(b), m, N.ptr(w), N.ptr(z), m, _stream()))
+    return w, z.t()
+
+
 def tridiag_pinv_solve_batch(alpha: torch.Tensor, beta: torch.Tensor, m, e0: torch.Tensor, c: torch.Tensor,
                              rhs: torch.Tensor) -> torch.Tensor:
     """v_b = -(T_b - e0_b)^+ rhs_b on the complement of c_b for B tridiagonals (c_b the unit

@@ -60,9 +60,9 @@ class EigenState(NamedTuple):
 
 
 def _dense_eigh(plan: E.Plan):
-    H = plan.dense()
-    w, v = torch.linalg.eigh(H)
-    return w, v
+    """Every eigenpair of a sector's dense Hamiltonian (solve_sector, exactdiag.py:46-57),
+    with the library's own FP64 eigensolver."""
+    return E.dense_eigh(plan.dense())
 
 
 def _sector_plan(model, n_up, n_dn) -> E.Plan:
@@ -379,10 +379,7 @@ def _tevo_part(model, gs, times: np.ndarray, pos: int, sigma: int, delta: int, n
     tt = E._as_dev_f64(times)
     if m == 0 or nrm == 0.0:
         return torch.zeros(tt.numel(), dtype=torch.complex128, device=E.device())
-    T = torch.diag(a)
-    if m > 1:
-        T = T + torch.diag(b[1:m], 1) + torch.diag(b[1:m], -1)
-    lam, U = torch.linalg.eigh(T)
+    lam, U = E.tridiag_eigh(a[:m], b[:m])
     w = (nrm * nrm) * U[0, :] ** 2
     return E.tevo_sum(lam, w, float(gs.energy), 1 if delta > 0 else -1, tt)
 

@@ -295,6 +295,24 @@ ED_API ed_status ed_tridiag_pinv_solve_batch(const double* d_alpha, int lda, con
                                              const int* d_m, int B, int max_m, const double* d_e0,
                                              const double* d_c, int ldc, const double* d_rhs, double* d_out,
                                              int ldr, ed_stream_t stream);
+/* Every eigenpair of B real symmetric matrices, FP64 (replaces numpy.linalg.eigh in
+ * solve_sector, cmpy/exactdiag.py:46-57, and the dense branch of exactdiag.py:24-43).
+ * Matrix b has order h_n[b] (host array, 1 <= h_n[b] <= n_max), row-major at
+ * d_a + b*stride_a with leading dimension lda, and is overwritten (Householder reflectors).
+ * Eigenvalues ascending -> d_w[b*n_max + i]; eigenvector i -> row i of
+ * d_z + b*stride_z (leading dimension ldz), i.e. Z = V^T. Degenerate eigenvalues get an
+ * orthonormal basis of their eigenspace. Asynchronous on `stream` (work memory from
+ * cudaMallocAsync: (4 + 5 n_max) B n_max doubles). */
+ED_API ed_status ed_dense_eigh_batch(double* d_a, int64_t lda, int64_t stride_a, const int* h_n, int B, int n_max,
+                                     double* d_w, double* d_z, int64_t ldz, int64_t stride_z,
+                                     ed_stream_t stream);
+/* Every eigenpair of the symmetric tridiagonal (d_alpha[0..m), d_beta[1..m)): eigenvalues
+ * ascending -> d_w, eigenvector i -> row i of d_z (leading dimension ldz). The same bisection
+ * and inverse iteration as ed_dense_eigh_batch; used for the real-time Green's function of a
+ * Lanczos tridiagonal (no reference counterpart: the reference's gf_greater/gf_lesser evolve
+ * states with expm_multiply, cmpy/exactdiag.py:280-330). Asynchronous on `stream`. */
+ED_API ed_status ed_tridiag_eigh(const double* d_alpha, const double* d_beta, int m, double* d_w, double* d_z,
+                                 int64_t ldz, ed_stream_t stream);
 
 /* ---- batched form: many sectors / realisations in one persistent launch -----------------
  * No reference counterpart: the reference solves sectors one after another on the host
