@@ -146,7 +146,24 @@ def case_sweep10() -> None:
     print(f"sweep10: {len(plans)} sectors, E0 = {float(r.energy.min()):.12f}")
 
 
-PROFILE_CASES = {"gf14": case_gf14, "adjoint64": case_adjoint64, "sweep10": case_sweep10}
+def case_gs14(steps: int = 250) -> None:
+    """The benchmark's ground-state run alone: 14-site ring (7,7), 250 block-fixed-point Lanczos
+    steps with the Ritz vector (Krylov store 23.6 GB), then the final tridiagonal eigenpair and
+    Ritz kernels; twice (the first run warms the plan and the workspace)."""
+    import torch
+
+    from cmpy_gb300 import engine as E
+
+    bonds = [(i, j, T) for i, j in sorted(ring_bonds(N_SITES))]
+    plan = E.Plan.fermion(N_SITES, [-MU] * N_SITES, [U] * N_SITES, bonds, N_UP, N_DN)
+    v0 = torch.rand(plan.dim, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(5))
+    for _ in range(2):
+        r = E.lanczos(plan, max_steps=steps, want_vector=True, v0=v0)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "gs14", "steps": r.steps, "energy": r.energy}))
+
+
+PROFILE_CASES = {"gf14": case_gf14, "adjoint64": case_adjoint64, "sweep10": case_sweep10, "gs14": case_gs14}
 
 
 def peaks():

@@ -1061,20 +1061,60 @@ __global__ void __launch_bounds__(BT, 4) k_bfp_update(BfpVecs v, int k, const in
 // psi = sum_k C_k R_k * 2^-SC (C_k and SC from the host: see bfp_lanczos)
 // (pu, pd non-null: the vectors are in the renumbered basis of the sweep or the stripe matvec
 // and psi is scattered back to the original order, nd = num_dn)
-__global__ void k_bfp_ritz(const BfpVecs v, const int64_t* __restrict__ C, const int* SCp, const BfpState* st,
-                           double* __restrict__ out, const int32_t* __restrict__ pu, const int32_t* __restrict__ pd,
-                           int64_t nd) {
+template <bool PAIRS>
+__global__ void __launch_bounds__(256) k_bfp_ritz(const BfpVecs v, const int64_t* __restrict__ C, const int* SCp,
+                                                  const BfpState* st, double* __restrict__ out,
+                                                  const int32_t* __restrict__ pu, const int32_t* __restrict__ pd,
+                                                  int64_t nd) {
   const int m = st->steps;
   const int SC = *SCp;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < v.D; i += (int64_t)gridDim.x * blockDim.x) {
-    I128 acc{0, 0};
-    for (int k = 0; k < m; ++k) add128(acc, mul_s64(C[k], v.vec(k)[i]));
+  const uint64_t first = policy_evict_first();  // every stored element is read once
+  auto put = [&](int64_t i, const I128& acc) {
     int64_t o = i;
     if (pu) {
       const int64_t r = i / nd, c = i - r * nd;
       o = (int64_t)__ldg(pu + r) * nd + __ldg(pd + c);
     }
     out[o] = ldexp(i128_to_double(acc), -SC);
+  };
+  if (PAIRS) {
+    // two adjacent elements per thread (16-byte loads; D even, store 16-byte aligned) and four
+    // Krylov vectors per loop step: 64 bytes of independent loads in flight per thread
+    const int64_t npairs = v.D >> 1;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < npairs; q += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t* base = v.R + 2 * q;
+      I128 a0{0, 0}, a1{0, 0};
+      int k = 0;
+      for (; k + 4 <= m; k += 4) {
+        const longlong2 x0 = ld2_stream(base + (int64_t)k * v.D, first);
+        const longlong2 x1 = ld2_stream(base + (int64_t)(k + 1) * v.D, first);
+        const longlong2 x2 = ld2_stream(base + (int64_t)(k + 2) * v.D, first);
+        const longlong2 x3 = ld2_stream(base + (int64_t)(k + 3) * v.D, first);
+        const int64_t c0 = __ldg(C + k), c1 = __ldg(C + k + 1), c2 = __ldg(C + k + 2), c3 = __ldg(C + k + 3);
+        add128(a0, mul_s64(c0, x0.x));
+        add128(a1, mul_s64(c0, x0.y));
+        add128(a0, mul_s64(c1, x1.x));
+        add128(a1, mul_s64(c1, x1.y));
+        add128(a0, mul_s64(c2, x2.x));
+        add128(a1, mul_s64(c2, x2.y));
+        add128(a0, mul_s64(c3, x3.x));
+        add128(a1, mul_s64(c3, x3.y));
+      }
+      for (; k < m; ++k) {
+        const longlong2 x = ld2_stream(base + (int64_t)k * v.D, first);
+        const int64_t c = __ldg(C + k);
+        add128(a0, mul_s64(c, x.x));
+        add128(a1, mul_s64(c, x.y));
+      }
+      put(2 * q, a0);
+      put(2 * q + 1, a1);
+    }
+  } else {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < v.D; i += (int64_t)gridDim.x * blockDim.x) {
+      I128 acc{0, 0};
+      for (int k = 0; k < m; ++k) add128(acc, mul_s64(C[k], v.vec(k)[i]));
+      put(i, acc);
+    }
   }
 }
 
@@ -1969,8 +2009,12 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
   ED_CHECK_LAUNCH("k_tri_final");
   if (evec) {
     k_bfp_ritz_coef<<<1, BT, 0, s>>>(r.c, beta, r.v.eR, r.tri, r.C, r.misc);
-    k_bfp_ritz<<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(
-        r.v, r.C, r.misc, r.st, evec, pu, pd, p->num_dn);
+    // (the stored vectors are 16-byte aligned when D is even: base 256-aligned, slots of D)
+    if (D % 2 == 0)
+      k_bfp_ritz<true><<<p->ctx->num_sms * 8, 256, 0, s>>>(r.v, r.C, r.misc, r.st, evec, pu, pd, p->num_dn);
+    else
+      k_bfp_ritz<false><<<grid_for(D, 256, p->ctx->num_sms * 8), 256, 0, s>>>(r.v, r.C, r.misc, r.st, evec, pu,
+                                                                            pd, p->num_dn);
     ED_CHECK_LAUNCH_N("k_bfp_ritz", 2);
   }
   BfpState hs;
