@@ -7,8 +7,10 @@
 //    the diagonal, p = tau A22 v, w = p - (tau/2)(p.v) v, A22 -= v w^T + w v^T. Each step is
 //    four launches over the whole batch (reflector, matrix-vector product with one warp per row,
 //    the dot product, rank-2 update), so a single large matrix uses every SM; the FP64 pipe of
-//    this GPU (two FMAs per clock per SM) bounds the O(n^3) parts. The rank-2 update is formed
-//    as v_i w_j + w_i v_j with separately rounded products, so A stays exactly symmetric.
+//    this GPU (two FMAs per clock per SM) bounds the O(n^3) parts. Batches of matrices of
+//    order <= 1024 take every step in one CTA per matrix instead (block barriers between the
+//    phases: no launch per step). The rank-2 update is formed as v_i w_j + w_i v_j with
+//    separately rounded products, so A stays exactly symmetric.
 // 2. All eigenvalues of T by bisection on Sturm counts (one thread per eigenvalue), ascending.
 // 3. Eigenvectors of T by inverse iteration (Gaussian elimination with partial pivoting of
 //    T - lambda I, start vectors that differ per index), one thread per cluster of eigenvalues
@@ -118,6 +120,72 @@ __global__ void __launch_bounds__(DE_NT) k_hh_update(DenseBatch m, int k) {
   double* ai = Ab + (size_t)i * m.lda;
   for (int j = k + 1 + threadIdx.x; j < n; j += DE_NT)
     ai[j] = __dsub_rn(ai[j], __dadd_rn(__dmul_rn(vi, w[j]), __dmul_rn(wi, v[j])));
+}
+
+// All Householder steps of one matrix per CTA (matrices of order <= DE_SMALL): the four phases
+// of a step separated by block barriers instead of launches. One SM's FP64 pipe does the
+// O(n^3) work, so this pays only for small orders: at n = 128 about 0.2 ms against ~1.5 ms of
+// per-step launches; at n = 300 the per-step launches over every SM are faster.
+constexpr int DE_SMALL = 128;
+constexpr int DE_NTS = 1024;
+__global__ void __launch_bounds__(DE_NTS) k_hh_small(DenseBatch m) {
+  __shared__ double sm[DE_NTS / 32];
+  __shared__ double sh_t, sh_k;
+  const int b = blockIdx.x, n = m.n[b];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double* Ab = m.A + (size_t)b * m.sa;
+  double* p = m.P + (size_t)b * m.nmax;
+  for (int k = 0; k + 3 <= n; ++k) {
+    double* v = Ab + (size_t)k * m.lda;
+    // reflector of row k
+    double s = 0.0;
+    for (int i = k + 2 + tid; i < n; i += DE_NTS) s = fma(v[i], v[i], s);
+    s = block_sum<DE_NTS>(s, sm);
+    if (tid == 0) {
+      const double x0 = v[k + 1];
+      double t = 0.0, alpha = x0;
+      if (s > 0.0) {
+        const double nrm = sqrt(fma(x0, x0, s));
+        alpha = x0 >= 0.0 ? -nrm : nrm;
+        const double v0 = x0 - alpha;
+        t = 2.0 / fma(v0, v0, s);
+        v[k + 1] = v0;
+      }
+      m.tau[(size_t)b * m.nmax + k] = t;
+      m.d[(size_t)b * m.nmax + k] = v[k];
+      m.bet[(size_t)b * m.nmax + k + 1] = alpha;
+      sh_t = t;
+    }
+    __syncthreads();
+    const double t = sh_t;
+    if (t == 0.0) continue;  // uniform: nothing to transform at this step
+    // p = tau A22 v, one warp per row
+    for (int i = k + 1 + warp; i < n; i += DE_NTS / 32) {
+      const double* ai = Ab + (size_t)i * m.lda;
+      double acc = 0.0;
+      for (int j = k + 1 + lane; j < n; j += 32) acc = fma(ai[j], v[j], acc);
+      acc = warp_sum_d(acc);
+      if (lane == 0) p[i] = t * acc;
+    }
+    __syncthreads();
+    // w = p - (tau/2)(p.v) v
+    double d = 0.0;
+    for (int i = k + 1 + tid; i < n; i += DE_NTS) d = fma(p[i], v[i], d);
+    d = block_sum<DE_NTS>(d, sm);
+    if (tid == 0) sh_k = 0.5 * t * d;
+    __syncthreads();
+    const double kk = sh_k;
+    for (int i = k + 1 + tid; i < n; i += DE_NTS) p[i] = fma(-kk, v[i], p[i]);
+    __syncthreads();
+    // A22 -= v w^T + w v^T (products rounded separately: A stays symmetric)
+    const int r = n - k - 1;
+    for (int e = tid; e < r * r; e += DE_NTS) {
+      const int i = k + 1 + e / r, j = k + 1 + e % r;
+      double* aij = Ab + (size_t)i * m.lda + j;
+      *aij = __dsub_rn(*aij, __dadd_rn(__dmul_rn(v[i], p[j]), __dmul_rn(p[i], v[j])));
+    }
+    __syncthreads();
+  }
 }
 
 // the last diagonal entries and the Gershgorin bounds of T (one thread per matrix)
@@ -346,7 +414,14 @@ ED_API ed_status ed_dense_eigh_batch(double* d_a, int64_t lda, int64_t stride_a,
   double* work = buf + 4 * nm + 2 * (size_t)B;
   ed_status st = ED_OK;
   const int rows_per = DE_NT / 32;
-  for (int k = 0; k + 3 <= n_max && st == ED_OK; ++k) {
+  if (n_max <= DE_SMALL) {
+    // every step of each matrix in one CTA
+    k_hh_small<<<B, DE_NTS, 0, s>>>(m);
+    const cudaError_t e = cudaGetLastError();
+    count_launches(1);
+    if (e != cudaSuccess) st = cuda_fail(e, "Householder (one CTA per matrix)");
+  }
+  for (int k = 0; n_max > DE_SMALL && k + 3 <= n_max && st == ED_OK; ++k) {
     const int rem = n_max - k - 1;
     k_hh_column<<<B, DE_NT, 0, s>>>(m, k);
     k_hh_matvec<<<dim3((rem + rows_per - 1) / rows_per, B), DE_NT, 0, s>>>(m, k);
@@ -358,10 +433,12 @@ ED_API ed_status ed_dense_eigh_batch(double* d_a, int64_t lda, int64_t stride_a,
   }
   if (st == ED_OK) {
     k_hh_finish<<<(B + 127) / 128, 128, 0, s>>>(m, B);
+    // one thread per eigenvalue in blocks of one warp: the bisections and inverse iterations
+    // are FP64 chains, so they are spread over as many SMs' FP64 pipes as possible
     const int64_t nt = (int64_t)B * n_max;
-    const int g1 = (int)((nt + 127) / 128);
-    k_tri_eigvals<<<g1, 128, 0, s>>>(m, B, d_w);
-    k_tri_eigvecs<<<g1, 128, 0, s>>>(m, B, d_w, d_z, ldz, stride_z, work);
+    const int g1 = (int)((nt + 31) / 32);
+    k_tri_eigvals<<<g1, 32, 0, s>>>(m, B, d_w);
+    k_tri_eigvecs<<<g1, 32, 0, s>>>(m, B, d_w, d_z, ldz, stride_z, work);
     k_hh_back<<<(int)((nt * 32 + DE_NT - 1) / DE_NT), DE_NT, 0, s>>>(m, B, d_z, ldz, stride_z);
     const cudaError_t e = cudaGetLastError();
     count_launches(4);
@@ -393,10 +470,10 @@ ED_API ed_status ed_tridiag_eigh(const double* d_alpha, const double* d_beta, in
   b.P = buf + 3 * (size_t)m;
   b.glim = buf + 4 * (size_t)m;
   b.nmax = m;
-  const int g1 = (m + 127) / 128;
+  const int g1 = (m + 31) / 32;
   k_tri_setup<<<1, 1, 0, s>>>(b, d_alpha, d_beta, m);
-  k_tri_eigvals<<<g1, 128, 0, s>>>(b, 1, d_w);
-  k_tri_eigvecs<<<g1, 128, 0, s>>>(b, 1, d_w, d_z, ldz, (int64_t)m * ldz, buf + 4 * (size_t)m + 2);
+  k_tri_eigvals<<<g1, 32, 0, s>>>(b, 1, d_w);
+  k_tri_eigvecs<<<g1, 32, 0, s>>>(b, 1, d_w, d_z, ldz, (int64_t)m * ldz, buf + 4 * (size_t)m + 2);
   const cudaError_t e = cudaGetLastError();
   count_launches(3);
   cudaFreeAsync(buf, s);

@@ -316,13 +316,15 @@ def gf_lehmann_zero_temperature(model, z, gs_energy: float, gs_state, n_up: int,
     zt = E._as_dev_c128(z)
     g = torch.zeros_like(zt)
     e0 = torch.tensor([gs_energy], dtype=torch.float64, device=E.device())
+    parts = []
     for delta, create in ((1, True), (-1, False)):
         nb = _neighbour(model, n_up, n_dn, sigma, delta)
-        if nb is None:
-            continue
-        tplan = _sector_plan(model, *nb)
-        phi = plan.apply_fermion(tplan, pos, sigma, create, psi, jw_sign=jw_sign)
-        w, v = _dense_eigh(tplan)
+        if nb is not None:
+            tplan = _sector_plan(model, *nb)
+            parts.append((create, tplan, plan.apply_fermion(tplan, pos, sigma, create, psi, jw_sign=jw_sign)))
+    # both neighbouring sectors in one call of the eigensolver
+    eig = E.dense_eigh_batch([tp.dense() for _, tp, _ in parts])
+    for (create, _, phi), (w, v) in zip(parts, eig):
         amp = (v.t() @ phi) ** 2  # |<m|phi>|^2
         if create:  # poles at E_m - E0, weights amp (Lehmann with unit ground-state weight)
             E.lehmann_accumulate(e0, w, amp.reshape(-1, 1), float("inf"), 0.0, zt, g)
