@@ -237,84 +237,4 @@ static __device__ void tridiag_pinv_solve(const double* a, const double* b, int 
   for (int i = 0; i < m; ++i) v[i] = -(v[i] - yc * c[i]);
 }
 
-// ---- the same on the host ----------------------------------------------------------------------
-// Lowest eigenpair of the tridiagonal (a[0..m), b[1..m)) on the host, FP64: bisection on the
-// Sturm count of the LDL^T pivots, then two steps of inverse iteration (Gaussian elimination
-// with partial pivoting); eigenvector sign: first nonzero component positive. The Lanczos
-// drivers use it for their convergence tests and final eigenpairs: the solve is a chain of
-// dependent FP64 operations, which this GPU's narrow FP64 pipe runs far slower (m = 250:
-// ~1.7 ms in one block) than a host core (tens of µs).
-inline double host_tridiag_lowest(const double* a, const double* b, int m, std::vector<double>& c) {
-  double lo = a[0], hi = a[0];
-  for (int i = 0; i < m; ++i) {
-    const double r = (i > 0 ? std::fabs(b[i]) : 0.0) + (i + 1 < m ? std::fabs(b[i + 1]) : 0.0);
-    lo = std::min(lo, a[i] - r);
-    hi = std::max(hi, a[i] + r);
-  }
-  const double pad = 1e-12 * std::max(std::fabs(lo), std::fabs(hi)) + 1e-300;
-  lo -= pad;
-  hi += pad;
-  auto count = [&](double x) {
-    int n = 0;
-    double q = a[0] - x;
-    for (int i = 0;;) {
-      if (q == 0.0) q = -1e-300;
-      if (q < 0.0) ++n;
-      if (++i >= m) break;
-      q = (a[i] - x) - b[i] * b[i] / q;
-    }
-    return n;
-  };
-  for (int it = 0; it < 200 && hi - lo > 4e-16 * std::max(std::fabs(lo), std::fabs(hi)) + 1e-300; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (count(mid) >= 1) hi = mid; else lo = mid;
-  }
-  const double ev = 0.5 * (lo + hi);
-  c.assign(m, 1.0 / std::sqrt((double)m));
-  for (int i = 0; i < m; ++i) c[i] *= 1.0 + 0.01 * (double)((i * 7919) % 13) / 13.0;
-  std::vector<double> dd(m), du(m), du2(m), ml(m);
-  std::vector<char> pv(m);
-  const double tiny = 1e-300 + 1e-18 * std::max(std::fabs(ev), 1.0);
-  for (int it = 0; it < 2; ++it) {
-    for (int i = 0; i < m; ++i) { dd[i] = a[i] - ev; du[i] = (i + 1 < m) ? b[i + 1] : 0.0; du2[i] = 0.0; }
-    for (int i = 0; i + 1 < m; ++i) {
-      const double sub = b[i + 1];
-      if (std::fabs(dd[i]) >= std::fabs(sub)) {
-        pv[i] = 0;
-        if (dd[i] == 0.0) dd[i] = tiny;
-        ml[i] = sub / dd[i];
-        dd[i + 1] -= ml[i] * du[i];
-      } else {
-        pv[i] = 1;
-        const double l = dd[i] / sub, t0 = dd[i + 1], t1 = (i + 2 < m) ? du[i + 1] : 0.0, odu = du[i];
-        ml[i] = l;
-        dd[i] = sub;
-        du[i] = t0;
-        du2[i] = t1;
-        dd[i + 1] = odu - l * t0;
-        if (i + 2 < m) du[i + 1] = -l * t1;
-      }
-    }
-    if (dd[m - 1] == 0.0) dd[m - 1] = tiny;
-    for (int i = 0; i + 1 < m; ++i) {
-      if (pv[i]) { const double t = c[i]; c[i] = c[i + 1]; c[i + 1] = t - ml[i] * c[i]; }
-      else c[i + 1] -= ml[i] * c[i];
-    }
-    for (int i = m - 1; i >= 0; --i) {
-      double s = c[i];
-      if (i + 1 < m) s -= du[i] * c[i + 1];
-      if (i + 2 < m) s -= du2[i] * c[i + 2];
-      c[i] = s / dd[i];
-    }
-    double nrm = 0.0;
-    for (int i = 0; i < m; ++i) nrm += c[i] * c[i];
-    nrm = 1.0 / std::sqrt(nrm);
-    for (int i = 0; i < m; ++i) c[i] *= nrm;
-  }
-  double sg = 1.0;
-  for (int i = 0; i < m; ++i) if (c[i] != 0.0) { sg = c[i] > 0 ? 1.0 : -1.0; break; }
-  for (int i = 0; i < m; ++i) c[i] *= sg;
-  return ev;
-}
-
 }  // namespace ed
