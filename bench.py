@@ -865,6 +865,74 @@ def run_chain6():
             "g_norm_check": float(-np.sum(g.imag) * (z[1].real - z[0].real) / np.pi)}
 
 
+def cpu_baseline_heisenberg():
+    """The reference's CPU path for the Heisenberg N=20 configuration (same couplings as
+    run_heisenberg): its triplets (the oracle's restatement of cmpy/models/heisenberg.py:19-40
+    with per-bond J) -> scipy CSR -> eigsh(k=1, which="SA", tol=1e-12) as in
+    cmpy/exactdiag.py:37, one host core, timed in full."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+
+    from oracle import ed_oracle as O
+
+    n = 20
+    rng = np.random.default_rng(0)
+    J = np.zeros((n, n))
+    for i in range(n):
+        k = (i + 1) % n
+        J[i, k] = J[k, i] = 1.0 + 0.1 * rng.standard_normal()
+    t0 = time.perf_counter()
+    states = O.sector_states(n, n // 2)
+    neighbors = [[(q - 1) % n, (q + 1) % n] for q in range(n)]
+    r, c, v = O.coo_heisenberg(states, O.heisenberg_pairs(neighbors, j=J, jz=J))
+    D = len(states)
+    H = sp.csr_matrix((v, (r, c)), shape=(D, D))
+    t1 = time.perf_counter()
+    e0 = float(sla.eigsh(H, k=1, which="SA", tol=1e-12, v0=np.random.default_rng(1).random(D),
+                         return_eigenvectors=False)[0])
+    t2 = time.perf_counter()
+    return {"kind": "port", "cores": 1, "gs_time_s": round(t2 - t0, 3),
+            "gs_parts_s": {"coo_csr_build": round(t1 - t0, 3), "eigsh": round(t2 - t1, 3)}, "gs_energy": e0,
+            "sample": "full configuration: reference triplets (oracle restatement) -> scipy CSR -> eigsh on one core"}
+
+
+def cpu_baseline_chain6():
+    """The reference's CPU path for config 1 (same model as run_chain6): dense sector
+    Hamiltonians from its triplets, numpy.linalg.eigh of the (3,3) sector for the ground state
+    and of the (4,3) and (2,3) sectors for the T=0 Lehmann sum at 512 frequencies
+    (cmpy/exactdiag.py:46-57, 215-245), one host core."""
+    from oracle import ed_oracle as O
+
+    n = 6
+    bonds = [[i, i + 1] for i in range(n - 1)]
+    eps, uu, bnd, width = O.hubbard_descriptor(n, bonds, inter=4.0, hop=1.0, mu=2.0)
+    z = np.linspace(-8, 8, 512) + 0.05j
+
+    def dense(nu, nd):
+        up, dn = O.sector_states(n, nu), O.sector_states(n, nd)
+        return up, dn, O.dense_from_coo(len(up) * len(dn), *O.coo_fermion(up, dn, eps, uu, bnd, width))
+
+    def run():
+        up, dn, H = dense(3, 3)
+        w, V = np.linalg.eigh(H)
+        psi = V[:, 0]
+        upp, dnp, Hp = dense(4, 3)
+        upm, dnm, Hm = dense(2, 3)
+        cd = O.apply_fermion(up, dn, upp, dn, 0, O.UP, True, psi)
+        cm = O.apply_fermion(up, dn, upm, dn, 0, O.UP, False, psi)
+        return w[0], O.gf_zero_temperature_dense(None, Hp, Hm, cd, cm, w[0], z)
+
+    run()
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        e0, g = run()
+    ms = 1e3 * (time.perf_counter() - t0) / reps
+    return {"kind": "port", "cores": 1, "ms": round(ms, 3), "gs_energy": float(e0),
+            "sample": "full configuration: reference triplets (oracle restatement) -> dense eigh of three sectors "
+                      "-> Lehmann sum at 512 frequencies, one host core, mean of 5"}
+
+
 def run_f64_matvec(steps: int = 20):
     """The FP64 matvec fallback: the 14-site (7,7) ring with t = 0.7 (not a dyadic hop, so the
     sector has no integer matvec), matvec launches timed inside an FP64 Lanczos run."""
@@ -917,6 +985,14 @@ def main():
                     out[key] = fn()
                 except Exception as exc:  # keep the headline line even if an extra fails
                     out[key] = {"error": f"{type(exc).__name__}: {exc}"}
+            # the reference's CPU path beside the two small configurations (cpu_baseline leg)
+            if not args.no_cpu_baseline:
+                for key, fn in (("heisenberg20", cpu_baseline_heisenberg), ("chain6_config1", cpu_baseline_chain6)):
+                    if isinstance(out.get(key), dict) and "error" not in out[key]:
+                        try:
+                            out[key]["cpu_baseline"] = fn()
+                        except Exception as exc:
+                            out[key]["cpu_baseline"] = {"error": f"{type(exc).__name__}: {exc}"}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.destroy_process_group()
