@@ -57,9 +57,10 @@ def parse():
 
 
 def run_matvec_only(n: int):
-    """N fixed-point Lanczos steps of the 14-site (7,7) sector per matvec variant (6 = two-pass
-    stripes, 5 = banded two-pass sweep, 3 = single-pass), the matvec launches timed with CUDA
-    events on the launching stream (one JSON line per variant)."""
+    """N fixed-point Lanczos steps of the 14-site (7,7) sector per matvec variant (7 = single-pass
+    with renumbered dn states, 6 = two-pass stripes, 5 = banded two-pass sweep, 3 = single-pass),
+    the matvec launches timed with CUDA events on the launching stream (one JSON line per
+    variant)."""
     import torch
 
     from cmpy_gb300 import engine as E
@@ -68,8 +69,9 @@ def run_matvec_only(n: int):
     plan = E.Plan.fermion(N_SITES, [-MU] * N_SITES, [U] * N_SITES, bonds, N_UP, N_DN)
     v0 = torch.rand(plan.dim, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(5))
     peak, _ = peaks()
-    kernels = {6: "k_stripe_up + k_stripe_dn", 5: "k_sweep_up + k_sweep_dn", 3: "k_bfp_hub_matvec3"}
-    for var in (6, 5, 3):
+    kernels = {7: "k_bfp_hub_matvec3 (dn renumbered, per-chunk lists)", 6: "k_stripe_up + k_stripe_dn",
+               5: "k_sweep_up + k_sweep_dn", 3: "k_bfp_hub_matvec3"}
+    for var in (7, 6, 5, 3):
         plan.set_matvec_variant(var)
         if plan.matvec_variant != var:
             continue
@@ -412,7 +414,9 @@ def run_ours(args, rank, world, dist):
             "unit": "GB/s",
             "frac": round(achieved / peak, 4) if achieved else None,
             "traffic": traffic,
-            "kernel": "k_bfp_hub_matvec3 (integer H·v, 16*D bytes per launch)",
+            "kernel": (f"k_bfp_hub_matvec3 (integer H·v, matvec variant {plan.matvec_variant}"
+                       f"{': dn states renumbered by hop count' if plan.matvec_variant == 7 else ''}, "
+                       "16*D bytes per launch)"),
             "peak_source": f"{peak_kind} (hbm_gbs, burst copy)",
             "matvec_us": round(mv_ms / mv_n * 1e3, 2) if mv_n else None,
         },

@@ -60,6 +60,21 @@ struct StripeTables {
   int pol = 0;                       // L2 policy selection (see ed_stripe.cuh)
 };
 
+// tables of variant 7: the single-pass matvec with the dn states renumbered by their numbers
+// of + and - hops (the up states keep their order), so that each 64-column chunk of a warp
+// loops over its own list lengths instead of every bond slot
+struct DnCompactTables {
+  int on = 0;
+  int rows = 0;                  // table words per column (largest + and - pair counts of a chunk)
+  uint32_t* tab = nullptr;       // [rows][nd]: two partner byte offsets (16 * column) per word
+  uint16_t* chunk = nullptr;     // [nd / 64]: + pairs | - pairs << 8 of each 64-column chunk
+  int32_t* perm_up = nullptr;    // [nu] identity
+  int32_t* perm_dn = nullptr;    // [nd] renumbered -> original dn index
+  uint64_t* s_dn = nullptr;      // dn states, renumbered
+  int32_t* e_dn = nullptr;       // diagonal mode 0 dn energies, renumbered
+  int64_t* f_dn = nullptr;       // diagonal mode 1 dn energies, renumbered
+};
+
 struct SweepTables {
   int on = 0;
   int ring_up = 0, ring_dn = 0;  // ring capacity in chunks of 32 rows (pass 1) / 32 columns (pass 2)
@@ -128,6 +143,7 @@ struct BfpTables {
   int32_t* e_dn_int = nullptr;  // [nd]
   SweepTables sw;
   StripeTables sp;
+  DnCompactTables dc;
   long wait_limit = 0;          // polls of a first bulk-copy wait before giving up (0: default)
   int force_var = 0;            // matvec variant chosen for this plan (0: automatic)
 };

@@ -228,9 +228,10 @@ class Plan:
 
     @property
     def matvec_variant(self) -> int:
-        """Fixed-point matvec the plan uses: 3/2/1 = single-pass kernels, 5 = banded two-pass
-        sweep (renumbered basis inside the Lanczos; only when forced or where 3 does not fit),
-        0 = none (FP64 matvec)."""
+        """Fixed-point matvec the plan uses: 7 = single-pass kernel with the dn states renumbered
+        by hop count (default where it fits), 3/2/1 = single-pass kernels in the sector's order,
+        5 = banded two-pass sweep, 6 = two-pass stripes (5 and 6 on request; 5, 6 and 7 keep the
+        Lanczos vectors in a renumbered basis), 0 = none (FP64 matvec)."""
         return int(N.lib().ed_plan_matvec_variant(self._h))
 
     def set_matvec_variant(self, variant: int) -> None:

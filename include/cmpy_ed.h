@@ -473,14 +473,16 @@ ED_API ed_status ed_fixed_to_f64(const int64_t* d_xm, int64_t n, int32_t exp, do
  * ed_plan_fixed_point, also returned in *h_m_in), output exponent *h_ew = ex - F. */
 ED_API ed_status ed_matvec_fixed(ed_plan plan, const int64_t* d_xm, int32_t ex, int64_t* d_wm,
                                  int32_t* h_ew, int* h_m_in, ed_stream_t stream);
-/* Which fixed-point matvec the plan uses (0: none). 3, 2, 1: single-pass kernels (3 where the
- * sector fits it). 5 is the banded two-pass sweep, chosen only when forced or where 3 does not
- * fit: the plan renumbers the up and the dn states (reverse Cuthill-McKee order of each spin's
- * hop graph) and its Lanczos runs keep their vectors in that basis; ed_matvec_fixed still takes
- * and returns vectors in the sector's ascending-state order. The environment variable
- * CMPY_ED_MATVEC=1..5 forces a variant where the sector allows it. */
+/* Which fixed-point matvec the plan uses (0: none). 7: the single-pass kernel with the dn
+ * states renumbered by their numbers of + and - hops (the default where its tables fit); 3, 2,
+ * 1: single-pass kernels in the sector's own order; 5: the banded two-pass sweep (up and dn
+ * states in reverse Cuthill-McKee order) and 6: two-pass stripes (states sorted by hop count),
+ * chosen when forced (5 also where 3 does not fit). Variants 5, 6 and 7 keep the vectors of
+ * their Lanczos runs in their renumbered basis; ed_matvec_fixed still takes and returns vectors
+ * in the sector's ascending-state order. All variants give bit-identical results. The
+ * environment variable CMPY_ED_MATVEC=1..7 forces a variant where the sector allows it. */
 ED_API int ed_plan_matvec_variant(ed_plan plan);
-/* Chooses the fixed-point matvec variant of this plan (0: automatic, 1..5 as above when the
+/* Chooses the fixed-point matvec variant of this plan (0: automatic, 1..7 as above when the
  * sector allows it, else the automatic choice); for comparisons and benchmarks. Takes effect
  * for the next call; not while a Lanczos run of the plan is in flight. */
 ED_API ed_status ed_plan_set_matvec_variant(ed_plan plan, int variant);

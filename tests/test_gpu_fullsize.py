@@ -69,13 +69,13 @@ print(json.dumps({"sum": int(torch.sum(w).item()), "sq": float(torch.sum((w.to(t
 def test_matvec_variants_identical(cuda):
     """Each variant in its own process (the variant is chosen once per process)."""
     outs = {}
-    for v in ("1", "2", "3", "4", "5", "6"):
+    for v in ("1", "2", "3", "4", "5", "6", "7"):
         env = dict(os.environ, CMPY_ED_MATVEC=v)
         r = subprocess.run([sys.executable, "-c", _VARIANT_SCRIPT, str(ROOT)], env=env, capture_output=True,
                            text=True, timeout=600)
         assert r.returncode == 0, r.stderr[-2000:]
         outs[v] = json.loads(r.stdout.strip().splitlines()[-1])
-    for v in ("2", "3", "4", "5", "6"):
+    for v in ("2", "3", "4", "5", "6", "7"):
         assert outs[v] == outs["1"], v
 
 

@@ -1,7 +1,7 @@
 """GPU parity of the banded two-pass fixed-point matvec (variant 5, the "sweep").
 
-* it is available on the benchmark sectors (the plans choose the faster single-pass kernel,
-  variant 3, by default) and its integer H·x equals variant 3's bit for bit, and the oracle's integer matrix on small sectors, for exact and
+* it is available on the benchmark sectors (the plans choose a faster single-pass variant by
+  default) and its integer H·x equals variant 3's bit for bit, and the oracle's integer matrix on small sectors, for exact and
   rounded (arbitrary on-site energy) diagonals;
 * a Lanczos run in its renumbered basis gives the same coefficients and ground state as the
   single-pass run, and the 12-site ring's ground-state energy measured on the reference;
@@ -45,16 +45,16 @@ CASES = [
 @pytest.mark.parametrize("name,mk,sec", CASES, ids=[c[0] for c in CASES])
 def test_sweep_bitexact_vs_single_pass(cuda, name, mk, sec):
     p = mk().plan(*sec)
-    assert p.matvec_variant == 3, name
     xm = _rand_mantissas(p, 7)
-    w3, e3 = p.matvec_fixed(xm, -10)
-    p.set_matvec_variant(5)
     try:
+        p.set_matvec_variant(3)
+        assert p.matvec_variant == 3, name
+        w3, e3 = p.matvec_fixed(xm, -10)
+        p.set_matvec_variant(5)
         assert p.matvec_variant == 5
         w5, e5 = p.matvec_fixed(xm, -10)
     finally:
         p.set_matvec_variant(0)
-    assert p.matvec_variant == 3
     assert e5 == e3
     assert torch.equal(w5, w3), (name, int((w5 != w3).sum()))
 
@@ -91,10 +91,11 @@ def test_sweep_lanczos_matches_single_pass(cuda):
     # reorthogonalisation turns rounding differences (here the reduction order of the dot
     # products) into different ghost copies: compare the coefficients before that
     kw = dict(max_steps=200, want_vector=True, v0=v0, tol=1e-12, check_every=10)
-    assert p.matvec_variant == 3
-    r3 = E.lanczos(p, **kw)
-    p.set_matvec_variant(5)
     try:
+        p.set_matvec_variant(3)
+        assert p.matvec_variant == 3
+        r3 = E.lanczos(p, **kw)
+        p.set_matvec_variant(5)
         assert p.matvec_variant == 5
         r5 = E.lanczos(p, **kw)
     finally:
