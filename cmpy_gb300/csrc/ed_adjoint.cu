@@ -394,9 +394,10 @@ ED_API ed_status ed_lanczos_tape(ed_plan p, const double* d_start, int max_steps
   double* cvec = scal + K + (K + 1);
   double* twork = cvec + (K + 2);
   double* n2 = twork + 5 * (K + 2);          // start norm^2
-  TriResult* tri = (TriResult*)(n2 + 2);
+  TriResult* tri = (TriResult*)(n2 + 2);  // 5 of the 16 scalars
   TapeState* st = (TapeState*)(base + L.off_state);
   ED_CUDA(cudaMemsetAsync(st, 0, sizeof(TapeState), s));
+  ED_CUDA(cudaMemsetAsync(tri, 0, sizeof(TriResult), s));  // no earlier test to start from
   ED_CUDA(cudaMemsetAsync(d_alpha, 0, K * sizeof(double), s));
   ED_CUDA(cudaMemsetAsync(d_beta, 0, (K + 1) * sizeof(double), s));
   const int gv = L.nparts;

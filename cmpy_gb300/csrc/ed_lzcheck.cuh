@@ -23,6 +23,7 @@ struct TriResult {
   int m_checked;    // size of the eigenpair held in cvec from the last check (0: none)
   int m_final;      // size of the final eigenproblem (0: the run stopped on an error)
   double e_checked;
+  double r_checked; // residual estimate of that check
   double energy;    // lowest eigenvalue of T_m_final
   double residual;  // |beta[m] c[m-1]|
 };
@@ -30,16 +31,30 @@ struct TriResult {
 constexpr int TRI_NT = 512;
 constexpr int TRI_SM = 512;  // tridiagonals up to this size are solved in shared memory
 
+// the bracket a test after a shorter run gives for the lowest eigenvalue of T_m: by
+// interlacing it is at most the earlier value; the earlier residual estimate sets how far below
+// it is looked for (the Sturm counts in tridiag_lowest_block confirm the bracket before use)
+__device__ __forceinline__ void tri_hint(const TriResult* tr, double* lo, double* hi) {
+  *lo = *hi = 0.0;
+  if (tr->m_checked <= 0) return;
+  const double e = tr->e_checked, s = fmax(1.0, fabs(e));
+  *hi = e + 1e-13 * s;
+  *lo = e - fmax(16.0 * tr->r_checked, 1e-9 * s);
+}
+
 // one convergence test after m steps (side stream)
 static __global__ void __launch_bounds__(TRI_NT) k_tri_check(const double* alpha, const double* beta, int m, double tol,
                                                             int* stop, int* steps, TriResult* tr, double* cvec,
                                                             double* work) {
   if (*(volatile int*)stop) return;  // converged, invariant subspace or failed wait already
-  const double e = tridiag_lowest_block<TRI_SM>(alpha, beta, m, cvec, work);
+  double lo, hi;
+  tri_hint(tr, &lo, &hi);
+  const double e = tridiag_lowest_block<TRI_SM>(alpha, beta, m, cvec, work, lo, hi);
   if (threadIdx.x == 0) {
     const double res = fabs(beta[m] * cvec[m - 1]);
     tr->m_checked = m;
     tr->e_checked = e;
+    tr->r_checked = res;
     if (res <= tol * fmax(1.0, fabs(e)) && atomicCAS(stop, 0, 1) == 0) *steps = m;
   }
 }
@@ -76,7 +91,9 @@ static __global__ void __launch_bounds__(TRI_NT) k_tri_final(const double* alpha
   if (tr->m_checked == m) {
     e = tr->e_checked;  // the vector of that check is still in cvec
   } else {
-    e = tridiag_lowest_block<TRI_SM>(alpha, beta, m, cvec, work);
+    double lo, hi;
+    tri_hint(tr, &lo, &hi);
+    e = tridiag_lowest_block<TRI_SM>(alpha, beta, m, cvec, work, lo, hi);
   }
   if (threadIdx.x == 0) {
     tr->m_final = m;

@@ -53,9 +53,14 @@ constexpr int MS_PTS = 128;
 // SM_M > 0 (single-block callers): for m <= SM_M the tridiagonal (with b^2), the elimination
 // work and the vector live in static shared memory instead of global memory. Batched callers
 // keep SM_M = 0.
+//
+// lo_hint < hi_hint (optional): a bracket of the lowest eigenvalue to start from (e.g. from a
+// convergence test of a shorter run of the same Lanczos recurrence); it is used only when the
+// Sturm counts confirm it (no eigenvalue below lo_hint, at least one below hi_hint), otherwise
+// the Gershgorin interval is.
 template <int SM_M = 0>
 static __device__ double tridiag_lowest_block(const double* a_g, const double* b_g, int m, double* vec_g,
-                                              double* work_g) {
+                                              double* work_g, double lo_hint = 0.0, double hi_hint = 0.0) {
   __shared__ double lo_s, hi_s;
   __shared__ int cnt_s[MS_PTS];
   const double* a = a_g;
@@ -83,6 +88,9 @@ static __device__ double tridiag_lowest_block(const double* a_g, const double* b
       in_smem = true;
     }
   }
+  const bool hinted = lo_hint < hi_hint;  // block-uniform
+  if (hinted && threadIdx.x < 2) cnt_s[threadIdx.x] = sturm_count(a, b, bb, m, threadIdx.x ? hi_hint : lo_hint);
+  __syncthreads();
   if (threadIdx.x == 0) {
     double lo = a[0], hi = a[0];
     for (int i = 0; i < m; ++i) {
@@ -93,6 +101,10 @@ static __device__ double tridiag_lowest_block(const double* a_g, const double* b
     const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
     lo_s = lo - pad;
     hi_s = hi + pad;
+    if (hinted && cnt_s[0] == 0 && cnt_s[1] >= 1) {
+      lo_s = fmax(lo_s, lo_hint);
+      hi_s = fmin(hi_s, hi_hint);
+    }
   }
   __syncthreads();
   for (int round = 0; round < 16; ++round) {
