@@ -275,10 +275,10 @@ def run_ours(args, rank, world, dist):
                       profile=profile)
         g = torch.zeros_like(zt)
         phi = plan.apply_fermion(plan_p, 0, 1, True, r.vector)
-        a, b, nrm = E.lanczos_coeffs(plan_p, phi, max_steps=GF_LEVELS)
-        E.continued_fraction(a, b, nrm * nrm, zt, e0=r.energy, sign=1, out=g)
         chi = plan.apply_fermion(plan_m, 0, 1, False, r.vector)
-        a2, b2, nrm2 = E.lanczos_coeffs(plan_m, chi, max_steps=GF_LEVELS)
+        # the particle and the hole run in one call (their steps interleave on the GPU)
+        (a, b, nrm), (a2, b2, nrm2) = E.lanczos_coeffs_multi([(plan_p, phi), (plan_m, chi)], max_steps=GF_LEVELS)
+        E.continued_fraction(a, b, nrm * nrm, zt, e0=r.energy, sign=1, out=g)
         E.continued_fraction(a2, b2, nrm2 * nrm2, zt, e0=r.energy, sign=-1, out=g)
         return r, g, (a.numel(), a2.numel())
 
@@ -358,10 +358,9 @@ def run_ours(args, rank, world, dist):
         r = E.lanczos(plan, max_steps=LZ_STEPS, want_vector=True, v0=vd, workspace=ws)
         g = torch.zeros_like(zd)
         phi = plan.apply_fermion(plan_p, 0, 1, True, r.vector)
-        a, b, nrm = E.lanczos_coeffs(plan_p, phi, max_steps=GF_LEVELS)
-        E.continued_fraction(a, b, nrm * nrm, zd, e0=r.energy, sign=1, out=g)
         chi = plan.apply_fermion(plan_m, 0, 1, False, r.vector)
-        a2, b2, nrm2 = E.lanczos_coeffs(plan_m, chi, max_steps=GF_LEVELS)
+        (a, b, nrm), (a2, b2, nrm2) = E.lanczos_coeffs_multi([(plan_p, phi), (plan_m, chi)], max_steps=GF_LEVELS)
+        E.continued_fraction(a, b, nrm * nrm, zd, e0=r.energy, sign=1, out=g)
         E.continued_fraction(a2, b2, nrm2 * nrm2, zd, e0=r.energy, sign=-1, out=g)
         h_psi.copy_(r.vector, non_blocking=True)
         h_g.copy_(g, non_blocking=True)

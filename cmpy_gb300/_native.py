@@ -140,6 +140,7 @@ _SIGNATURES = {
         [PLAN, C.POINTER(LanczosParams), P, P, C.c_size_t, P, P, P, C.POINTER(LanczosResult), P],
     ),
     "ed_lanczos_coeffs": (I32, [PLAN, I32, P, P, C.c_size_t, P, P, C.POINTER(I32), C.POINTER(F64), P]),
+    "ed_lanczos_coeffs_multi": (I32, [I32, P, I32, P, P, P, P, P, P, P, P]),
     "ed_tridiag_lowest": (I32, [P, P, I32, P, P, P]),
     "ed_tridiag_lowest_noalloc": (I32, [P, P, I32, P, P, P]),
     "ed_tridiag_lowest_batch": (I32, [P, I32, P, I32, P, I32, I32, P, P, I32, P]),

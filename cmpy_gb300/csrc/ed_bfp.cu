@@ -2174,14 +2174,28 @@ ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const do
   return ED_OK;
 }
 
-ed_status bfp_lanczos_coeffs(const ed_plan_s* p, int K, const double* start, void* work, double* alpha,
-                             double* beta, int* steps, double* norm, cudaStream_t s) {
+// a coefficient run in three parts, so that several independent runs can interleave their
+// steps on separate streams (bfp_lanczos_coeffs_multi)
+struct BfpCoeffRun {
+  const ed_plan_s* p;
+  BfpRun r;
+  double *alpha, *beta;
+  int Km = 0;
+  bool empty = false;  // zero start vector: an empty Krylov space
+};
+
+// memsets, the start vector's finiteness and zero test (synchronous on s), R_0 and beta_0
+static ed_status bfp_coeffs_begin(const ed_plan_s* p, int K, const double* start, void* work, double* alpha,
+                                  double* beta, cudaStream_t s, BfpCoeffRun* run) {
   const int64_t D = p->dim;
-  BfpRun r = bfp_bind(p, work, K, false);
+  run->p = p;
+  run->r = bfp_bind(p, work, K, false);
+  run->alpha = alpha;
+  run->beta = beta;
+  BfpRun& r = run->r;
   ED_CUDA(cudaMemsetAsync(r.st, 0, sizeof(BfpState), s));
   ED_CUDA(cudaMemsetAsync(alpha, 0, K * sizeof(double), s));
   ED_CUDA(cudaMemsetAsync(beta, 0, (K + 1) * sizeof(double), s));
-  // a zero start vector has an empty Krylov space
   {
     const int gs = grid_for(D, 256, p->ctx->num_sms * 8);
     unsigned long long* mxb = (unsigned long long*)(r.misc + 8);
@@ -2193,24 +2207,84 @@ ed_status bfp_lanczos_coeffs(const ed_plan_s* p, int K, const double* start, voi
     ED_CUDA(cudaStreamSynchronize(s));
     const double mx = *(double*)&hm;
     if (!std::isfinite(mx)) return fail(ED_ERR_NONFINITE, "start vector is not finite");
-    if (mx == 0.0) { *steps = 0; *norm = 0.0; return ED_OK; }
+    if (mx == 0.0) {
+      run->empty = true;
+      return ED_OK;
+    }
   }
   const int32_t *pu, *pd;
   (void)matvec_perms(p, &pu, &pd);
   ED_TRY(bfp_start(p, r, start, beta, s, pu, pd));
-  const int Km = (int)std::min<int64_t>(K, D);
-  for (int k = 0; k < Km; ++k) ED_TRY(bfp_step(p, r, k, alpha, beta, s));
+  run->Km = (int)std::min<int64_t>(K, D);
+  return ED_OK;
+}
+
+// the run's steps and norm once its stream has finished (synchronous on s)
+static ed_status bfp_coeffs_end(BfpCoeffRun& run, int* steps, double* norm, cudaStream_t s) {
+  if (run.empty) {
+    *steps = 0;
+    *norm = 0.0;
+    return ED_OK;
+  }
   BfpState hs;
   double b0 = 0.0;
-  ED_CUDA(cudaMemcpyAsync(&hs, r.st, sizeof(BfpState), cudaMemcpyDeviceToHost, s));
-  ED_CUDA(cudaMemcpyAsync(&b0, beta, sizeof(double), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(&hs, run.r.st, sizeof(BfpState), cudaMemcpyDeviceToHost, s));
+  ED_CUDA(cudaMemcpyAsync(&b0, run.beta, sizeof(double), cudaMemcpyDeviceToHost, s));
   ED_CUDA(cudaStreamSynchronize(s));
   if (hs.status == DEV_TIMEOUT) return fail(ED_ERR_TIMEOUT, "fixed-point matvec: a bounded wait for a row copy ran out");
-  *steps = hs.stop ? hs.steps : Km;
+  *steps = hs.stop ? hs.steps : run.Km;
   *norm = b0;
   // the continued fraction expects beta[0] = 0 and beta[k] the couplings
-  ED_CUDA(cudaMemsetAsync(beta, 0, sizeof(double), s));
+  ED_CUDA(cudaMemsetAsync(run.beta, 0, sizeof(double), s));
+  ED_CUDA(cudaStreamSynchronize(s));
   return ED_OK;
+}
+
+ed_status bfp_lanczos_coeffs(const ed_plan_s* p, int K, const double* start, void* work, double* alpha,
+                             double* beta, int* steps, double* norm, cudaStream_t s) {
+  BfpCoeffRun run;
+  ED_TRY(bfp_coeffs_begin(p, K, start, work, alpha, beta, s, &run));
+  for (int k = 0; k < run.Km; ++k) ED_TRY(bfp_step(p, run.r, k, alpha, beta, s));
+  return bfp_coeffs_end(run, steps, norm, s);
+}
+
+// n independent coefficient runs with interleaved steps: run i on its own stream, forked from
+// and joined back into s. Each step of a run is two kernels that each fill the GPU for most
+// of their time; interleaving lets one run's kernels start on the SMs that the other run's
+// last partial round leaves idle. Results are those of the runs done one after another.
+ed_status bfp_lanczos_coeffs_multi(int n, const ed_plan_s* const* plans, int K, const double* const* starts,
+                                   void* const* works, double* const* alphas, double* const* betas, int* steps,
+                                   double* norms, cudaStream_t s) {
+  std::vector<cudaStream_t> ss(n, nullptr);
+  std::vector<BfpCoeffRun> runs(n);
+  cudaEvent_t fork = nullptr;
+  ed_status st = ED_OK;
+  auto cleanup = [&]() {
+    for (auto& x : ss)
+      if (x) cudaStreamDestroy(x);
+    if (fork) cudaEventDestroy(fork);
+  };
+  auto check = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && st == ED_OK) st = cuda_fail(e, what);
+  };
+  check(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreateWithFlags");
+  if (st == ED_OK) check(cudaEventRecord(fork, s), "cudaEventRecord");
+  for (int i = 0; i < n && st == ED_OK; ++i) {
+    check(cudaStreamCreateWithFlags(&ss[i], cudaStreamNonBlocking), "cudaStreamCreateWithFlags");
+    if (st == ED_OK) check(cudaStreamWaitEvent(ss[i], fork, 0), "cudaStreamWaitEvent");
+    if (st == ED_OK) st = bfp_coeffs_begin(plans[i], K, starts[i], works[i], alphas[i], betas[i], ss[i], &runs[i]);
+  }
+  int kmax = 0;
+  for (int i = 0; i < n && st == ED_OK; ++i) kmax = std::max(kmax, runs[i].Km);
+  for (int k = 0; k < kmax && st == ED_OK; ++k)
+    for (int i = 0; i < n && st == ED_OK; ++i)
+      if (k < runs[i].Km) st = bfp_step(runs[i].p, runs[i].r, k, runs[i].alpha, runs[i].beta, ss[i]);
+  for (int i = 0; i < n && st == ED_OK; ++i) st = bfp_coeffs_end(runs[i], &steps[i], &norms[i], ss[i]);
+  if (st != ED_OK)
+    for (auto& x : ss)
+      if (x) cudaStreamSynchronize(x);  // nothing of a failed call stays in flight
+  cleanup();
+  return st;
 }
 
 }  // namespace ed

@@ -574,6 +574,39 @@ ED_API ed_status ed_lanczos(ed_plan p, const ed_lanczos_params* prm, const doubl
   return ED_OK;
 }
 
+ED_API ed_status ed_lanczos_coeffs_multi(int n, const ed_plan* plans, int K, const double* const* d_starts,
+                                         void* const* d_work, const size_t* work_bytes, double* const* d_alpha,
+                                         double* const* d_beta, int* h_steps, double* h_norm, ed_stream_t stream) {
+  if (n < 1 || !plans || !d_starts || !d_work || !work_bytes || !d_alpha || !d_beta || !h_steps || !h_norm)
+    return fail(ED_ERR_INVALID_ARG, "null argument or n < 1");
+  if (K < 1 || K > 4096) return fail(ED_ERR_INVALID_ARG, "max_steps must be in [1, 4096]");
+  bool all_fixed = true;
+  for (int i = 0; i < n; ++i) {
+    ED_TRY(check_plan(plans[i]));
+    if (!d_starts[i] || !d_alpha[i] || !d_beta[i]) return fail(ED_ERR_INVALID_ARG, "null argument");
+    if (plans[i]->dim < 1) return fail(ED_ERR_INVALID_ARG, "empty sector");
+    if (plans[i]->bfp.eligible) {
+      if (!d_work[i] || work_bytes[i] < bfp_workspace_bytes(plans[i], K, false))
+        return fail(ED_ERR_INVALID_ARG, "workspace too small (see ed_lanczos_workspace)");
+    } else {
+      all_fixed = false;
+    }
+    for (int j = 0; j < i; ++j)
+      if (d_work[j] == d_work[i] || d_alpha[j] == d_alpha[i] || d_beta[j] == d_beta[i])
+        return fail(ED_ERR_INVALID_ARG, "the runs must not share workspaces or outputs");
+  }
+  if (!all_fixed) {
+    // FP64 runs: one after another on the caller's stream
+    for (int i = 0; i < n; ++i)
+      ED_TRY(ed_lanczos_coeffs(plans[i], K, d_starts[i], d_work[i], work_bytes[i], d_alpha[i], d_beta[i],
+                               &h_steps[i], &h_norm[i], stream));
+    return ED_OK;
+  }
+  std::vector<const ed_plan_s*> ps(plans, plans + n);
+  return bfp_lanczos_coeffs_multi(n, ps.data(), K, d_starts, d_work, d_alpha, d_beta, h_steps, h_norm,
+                                  as_stream(stream));
+}
+
 ED_API ed_status ed_lanczos_coeffs(ed_plan p, int K, const double* d_start, void* d_work, size_t work_bytes,
                                    double* d_alpha, double* d_beta, int* h_steps, double* h_norm, ed_stream_t stream) {
   ED_TRY(check_plan(p));

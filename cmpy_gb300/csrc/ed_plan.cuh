@@ -187,6 +187,9 @@ size_t bfp_workspace_bytes(const ed_plan_s* p, int K, bool store);
 ed_status bfp_lanczos(const ed_plan_s* p, const ed_lanczos_params* prm, const double* v0_dev, void* work,
                       double* alpha, double* beta, double* evec, ed_lanczos_result* res, cudaStream_t s,
                       double* v0_tmp);
+ed_status bfp_lanczos_coeffs_multi(int n, const ed_plan_s* const* plans, int K, const double* const* starts,
+                                   void* const* works, double* const* alphas, double* const* betas, int* steps,
+                                   double* norms, cudaStream_t s);
 ed_status bfp_lanczos_coeffs(const ed_plan_s* p, int K, const double* start, void* work, double* alpha,
                              double* beta, int* steps, double* norm, cudaStream_t s);
 }  // namespace ed

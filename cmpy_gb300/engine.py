@@ -470,6 +470,46 @@ def lanczos_coeffs(plan: Plan, start: torch.Tensor, max_steps: int = 200,
         return alpha[:m], beta[: m + 1], float(nrm.value)
 
 
+def lanczos_coeffs_multi(runs, max_steps: int = 200) -> list[tuple[torch.Tensor, torch.Tensor, float]]:
+    """lanczos_coeffs for several independent (plan, start) pairs in one call: with fixed-point
+    plans their steps interleave on separate streams (one run's kernels fill the SMs the other
+    leaves idle); the results equal separate lanczos_coeffs calls."""
+    runs = list(runs)
+    if not runs:
+        return []
+    L = N.lib()
+    prm = N.LanczosParams()
+    prm.max_steps = int(max_steps)
+    n = len(runs)
+    with runs[0][0]._dev():
+        keep, starts, works, sizes, alphas, betas = [], [], [], [], [], []
+        for plan, start in runs:
+            nb = C.c_size_t()
+            N.check(L.ed_lanczos_workspace(plan.handle, C.byref(prm), C.byref(nb)))
+            w = torch.empty(max(int(nb.value), 1), dtype=torch.uint8, device=device())
+            s = _as_dev_f64(start).reshape(-1).contiguous()
+            a = torch.empty(prm.max_steps, dtype=torch.float64, device=device())
+            b = torch.empty(prm.max_steps + 1, dtype=torch.float64, device=device())
+            keep += [w, s, a, b]
+            starts.append(N.ptr(s))
+            works.append(N.ptr(w))
+            sizes.append(int(nb.value))
+            alphas.append(N.ptr(a))
+            betas.append(N.ptr(b))
+        P = C.c_void_p
+        h_plans = (P * n)(*[p.handle for p, _ in runs])
+        h_steps = (C.c_int * n)()
+        h_norm = (C.c_double * n)()
+        N.check(L.ed_lanczos_coeffs_multi(n, h_plans, prm.max_steps, (P * n)(*starts), (P * n)(*works),
+                                          (C.c_size_t * n)(*sizes), (P * n)(*alphas), (P * n)(*betas), h_steps,
+                                          h_norm, _stream()))
+        out = []
+        for i in range(n):
+            m = int(h_steps[i])
+            out.append((keep[4 * i + 2][:m], keep[4 * i + 3][: m + 1], float(h_norm[i])))
+        return out
+
+
 def tridiag_lowest(alpha, beta, want_vector: bool = True):
     """Lowest eigenpair of the tridiagonal (alpha[0..m), beta[1..m)) on the device."""
     a = _as_dev_f64(alpha).reshape(-1)

@@ -343,17 +343,22 @@ def gf_continued_fraction(model, z, n_up: int, n_dn: int, gs_energy: float, gs_s
     zt = E._as_dev_c128(z)
     g = torch.zeros_like(zt)
     coeffs = {}
+    parts = []
     for delta, create, sign in ((1, True, 1), (-1, False, -1)):
         nb = _neighbour(model, n_up, n_dn, sigma, delta)
         if nb is None:
             continue
         tplan = _sector_plan(model, *nb)
-        phi = plan.apply_fermion(tplan, pos, sigma, create, psi, jw_sign=jw_sign)
-        a, b, nrm = E.lanczos_coeffs(tplan, phi, max_steps=min(n_lev, tplan.dim))
-        coeffs["particle" if create else "hole"] = (a, b, nrm)
-        if a.numel() == 0:
-            continue
-        E.continued_fraction(a, b, nrm * nrm, zt, e0=gs_energy, sign=sign, out=g)
+        parts.append((create, sign, tplan, plan.apply_fermion(tplan, pos, sigma, create, psi, jw_sign=jw_sign)))
+    if parts:
+        # the particle and the hole run in one call: their steps interleave on the GPU
+        K = min(n_lev, max(tp.dim for _, _, tp, _ in parts))
+        runs = E.lanczos_coeffs_multi([(tp, phi) for _, _, tp, phi in parts], max_steps=K)
+        for (create, sign, _, _), (a, b, nrm) in zip(parts, runs):
+            coeffs["particle" if create else "hole"] = (a, b, nrm)
+            if a.numel() == 0:
+                continue
+            E.continued_fraction(a, b, nrm * nrm, zt, e0=gs_energy, sign=sign, out=g)
     out = g.cpu().numpy()
     return (out, coeffs) if return_coeffs else out
 

@@ -274,6 +274,17 @@ ED_API ed_status ed_lanczos_coeffs(ed_plan plan, int max_steps, const double* d_
                                    void* d_work, size_t work_bytes, double* d_alpha,
                                    double* d_beta, int* h_steps, double* h_norm,
                                    ed_stream_t stream);
+/* n independent ed_lanczos_coeffs runs in one call (e.g. the particle and the hole part of a
+ * Green's function, cmpy/exactdiag.py:215-245 takes both from one ground state): with
+ * fixed-point plans their steps interleave on n internal streams forked from `stream`, so one
+ * run's kernels fill the SMs that the other's leave idle; results equal the runs done one after
+ * another. Run i: plans[i], d_starts[i], d_work[i] (work_bytes[i]), d_alpha[i], d_beta[i] ->
+ * h_steps[i], h_norm[i]; workspaces and outputs must be distinct. Synchronous. */
+ED_API ed_status ed_lanczos_coeffs_multi(int n, const ed_plan* plans, int max_steps,
+                                         const double* const* d_starts, void* const* d_work,
+                                         const size_t* work_bytes, double* const* d_alpha,
+                                         double* const* d_beta, int* h_steps, double* h_norm,
+                                         ed_stream_t stream);
 
 /* Lowest eigenpair of the symmetric tridiagonal matrix (alpha[0..m), beta[1..m)) on the
  * device, FP64 (replaces scipy.linalg.eigh_tridiagonal in cmpy/exactdiag.py:368-375).

@@ -135,3 +135,27 @@ def test_stripe_gf_coefficients_match_single_pass(cuda):
     # differently, and 40 steps from a random start amplify that little
     np.testing.assert_allclose(a6.cpu().numpy(), a3.cpu().numpy(), rtol=1e-10, atol=1e-10)
     np.testing.assert_allclose(b6.cpu().numpy(), b3.cpu().numpy(), rtol=1e-10, atol=1e-10)
+
+
+def test_coefficient_runs_interleaved_equal_separate(cuda):
+    """ed_lanczos_coeffs_multi: the particle and hole runs of the 14-site ground-state Green's
+    function (sectors (8,7) and (6,7)) with interleaved steps give exactly the coefficients of
+    separate runs; so do an FP64 plan (non-dyadic t) mixed in and a zero start vector."""
+    from cmpy_gb300 import engine as E
+
+    m = _hub(14, True, inter=4.0, mu=2.0)
+    pp, pm = m.plan(8, 7), m.plan(6, 7)
+    g = torch.Generator(device="cuda").manual_seed(8)
+    s1 = torch.rand(pp.dim, dtype=torch.float64, device="cuda", generator=g)
+    s2 = torch.rand(pm.dim, dtype=torch.float64, device="cuda", generator=g)
+    sep = [E.lanczos_coeffs(pp, s1, max_steps=60), E.lanczos_coeffs(pm, s2, max_steps=60)]
+    mult = E.lanczos_coeffs_multi([(pp, s1), (pm, s2)], max_steps=60)
+    for (a, b, n), (a2, b2, n2) in zip(sep, mult):
+        assert torch.equal(a, a2) and torch.equal(b, b2) and n == n2
+    small = _hub(8, True, inter=4.0, mu=2.0, hop=0.7).plan(4, 4)  # no integer matvec
+    z = torch.zeros(small.dim, dtype=torch.float64, device="cuda")
+    s3 = torch.rand(small.dim, dtype=torch.float64, device="cuda", generator=g)
+    out = E.lanczos_coeffs_multi([(small, s3), (small, z)], max_steps=40)
+    ref = E.lanczos_coeffs(small, s3, max_steps=40)
+    assert torch.equal(out[0][0], ref[0]) and torch.equal(out[0][1], ref[1])
+    assert out[1][0].numel() == 0 and out[1][2] == 0.0
