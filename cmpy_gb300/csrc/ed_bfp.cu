@@ -647,7 +647,8 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
   extern __shared__ __align__(128) unsigned char sm3[];
   __shared__ double smd[MV3_MAXNT / 32];
   __shared__ unsigned long long smu[MV3_MAXNT / 32];
-  const int64_t nd = a.nd, nu = a.nu;
+  // element offsets in 32 bits: the kernel is chosen only for dim < 2^31 and nd < 4096
+  const int nd = (int)a.nd, nu = (int)a.nu;
   const Mv3Layout L = mv3_layout(nd, n_b2, max_up);
   int64_t* raw = (int64_t*)(sm3 + L.raw_off);          // [MV3_R][nd]
   longlong2* xs2 = (longlong2*)(sm3 + L.xs_off);       // [nd + 1]
@@ -656,19 +657,19 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
   int32_t* cnt = (int32_t*)(sm3 + L.cnt_off);          // [2][MV3_R][4]: + len, - len, pad correction
   uint64_t* bar = (uint64_t*)(sm3 + L.bar_off);
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int64_t ngroups = (nu + MV3_R - 1) / MV3_R;
+  const int ngroups = (nu + MV3_R - 1) / MV3_R;
   const uint64_t keep = policy_evict_last(), stream = policy_evict_first();
 
   // stage group g from thread 0: bulk copies of its rows into `raw` and of its precomputed
   // padded up-lists and counts (rows u0, u0 + 1; row nu is an empty list) into list buffer s.
   // Everything lands on one mbarrier phase; no other thread waits on global loads here.
-  auto stage = [&](int64_t g, int s) {
+  auto stage = [&](int g, int s) {
     if (tid == 0) mv3_stage<UPW>(g, s, nu, nd, L.lstride, X, up_lst, up_cnt, raw, lst, cnt, bar);
   };
 
   // one-time set-up: the table, the zero slot pair, the barrier
   {
-    for (int64_t i = tid; i < (int64_t)n_b2 * nd; i += nt) tab[i] = __ldg(btab2 + i);
+    for (int i = tid; i < n_b2 * nd; i += nt) tab[i] = __ldg(btab2 + i);
     if (tid == 0) {
       xs2[nd] = make_longlong2(0, 0);
       mbar_init(bar, 1);
@@ -678,7 +679,7 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
   }
   bool pending = false;  // a bulk copy into `raw` has been issued and not yet waited for
   unsigned par = 0u;     // parity of the barrier's next phase completion
-  if ((int64_t)blockIdx.x < ngroups) {
+  if ((int)blockIdx.x < ngroups) {
     stage(blockIdx.x, 0);
     pending = true;
   }
@@ -688,10 +689,11 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
   unsigned long long mx = 0;
   bool bad = false;
   int k = 0;
-  for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x, ++k) {
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  for (int g = blockIdx.x; g < ngroups; g += gridDim.x, ++k) {
     const int s = k & 1;
-    const int64_t row0 = g * MV3_R;
-    const int nr = (int)min((int64_t)MV3_R, nu - row0);
+    const int row0 = g * MV3_R;
+    const int nr = min(MV3_R, nu - row0);
     if (mbar_wait_polls(bar, par, wait_limit)) {
       pending = false;
       par ^= 1u;
@@ -703,9 +705,9 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
       break;
     }
     // interleave the landed rows (a missing second row reads as zeros)
-    for (int64_t c = tid; c < nd; c += nt) xs2[c] = make_longlong2(raw[c], nr > 1 ? raw[nd + c] : 0);
+    for (int c = tid; c < nd; c += nt) xs2[c] = make_longlong2(raw[c], nr > 1 ? raw[nd + c] : 0);
     __syncthreads();  // xs2 complete; raw free for the next group's copy
-    const int64_t gn = g + gridDim.x;
+    const int gn = g + gridDim.x;
     if (gn < ngroups) {
       stage(gn, s ^ 1);  // list buffer s^1 was released by the barrier that ended step k-1
       pending = true;
@@ -714,16 +716,18 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
     const int32_t* l1 = lst + (s * MV3_R + 1) * L.lstride;
     const int32_t cp0 = UPW ? 0 : cnt[(s * MV3_R + 0) * 4 + 0], cn0 = UPW ? 0 : cnt[(s * MV3_R + 0) * 4 + 1];
     const int32_t cp1 = UPW ? 0 : cnt[(s * MV3_R + 1) * 4 + 0], cn1 = UPW ? 0 : cnt[(s * MV3_R + 1) * 4 + 1];
-    const int64_t corr0 = UPW ? 0 : cnt[(s * MV3_R + 0) * 4 + 2], corr1 = UPW ? 0 : cnt[(s * MV3_R + 1) * 4 + 2];
-    const uint64_t su0 = __ldg(a.up_states + row0), su1 = __ldg(a.up_states + row0 + (nr > 1 ? 1 : 0));
+    const int32_t corr0 = UPW ? 0 : cnt[(s * MV3_R + 0) * 4 + 2], corr1 = UPW ? 0 : cnt[(s * MV3_R + 1) * 4 + 2];
+    const int row1 = row0 + (nr > 1 ? 1 : 0);
+    const uint64_t su0 = __ldg(a.up_states + row0), su1 = __ldg(a.up_states + row1);
     const int64_t eu0 = DIAG64 ? 0 : (int64_t)__ldg(a.e_up + row0);
-    const int64_t eu1 = DIAG64 ? 0 : (int64_t)__ldg(a.e_up + row0 + (nr > 1 ? 1 : 0));
+    const int64_t eu1 = DIAG64 ? 0 : (int64_t)__ldg(a.e_up + row1);
     const int64_t ef0 = DIAG64 ? __ldg(a.e_up_fx + row0) : 0;
-    const int64_t ef1 = DIAG64 ? __ldg(a.e_up_fx + row0 + (nr > 1 ? 1 : 0)) : 0;
-    const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+    const int64_t ef1 = DIAG64 ? __ldg(a.e_up_fx + row1) : 0;
+    // element offset of the group's first row (the second row, o0 + nd, is touched only when nr > 1)
+    const int o0 = row0 * nd;
     const int n0 = cp0 + cn0, n1 = cp1 + cn1, nmax = max(n0, n1);
     // warps take 64-column chunks; lane l owns columns base + l and base + 32 + l
-    for (int64_t base = (int64_t)warp * 64; base < nd; base += (int64_t)nwarp * 64) {
+    for (int base = warp * 64; base < nd; base += nwarp * 64) {
       // dn table rows of this chunk: + pairs [0, np), - pairs [np, ne) (variant 7: per chunk)
       int np = n_b2pos, ne = n_b2;
       if (CMP) {
@@ -732,21 +736,20 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
         ne = np + (int)(cc >> 8);
       }
       // the chunk's per-column data, requested early
-      const int64_t c_lo = min(base + lane, nd - 1), c_hi = min(base + 32 + lane, nd - 1);
+      const int c_lo = min(base + lane, nd - 1), c_hi = min(base + 32 + lane, nd - 1);
       const uint64_t sd_lo = __ldg(a.dn_states + c_lo), sd_hi = __ldg(a.dn_states + c_hi);
       const int32_t e32_lo = DIAG64 ? 0 : __ldg(a.e_dn + c_lo), e32_hi = DIAG64 ? 0 : __ldg(a.e_dn + c_hi);
       const int64_t e64_lo = DIAG64 ? __ldg(a.e_dn_fx + c_lo) : 0, e64_hi = DIAG64 ? __ldg(a.e_dn_fx + c_hi) : 0;
       int64_t up_lo[2], up_hi[2];
       if (UPW) {
         // the up-neighbour sums of the two rows, written by the panel pass
-        up_lo[0] = W[row0 * nd + c_lo];
-        up_hi[0] = W[row0 * nd + c_hi];
-        up_lo[1] = nr > 1 ? W[(row0 + 1) * nd + c_lo] : 0;
-        up_hi[1] = nr > 1 ? W[(row0 + 1) * nd + c_hi] : 0;
+        up_lo[0] = W[o0 + c_lo];
+        up_hi[0] = W[o0 + c_hi];
+        up_lo[1] = nr > 1 ? W[o0 + nd + c_lo] : 0;
+        up_hi[1] = nr > 1 ? W[o0 + nd + c_hi] : 0;
       } else {
       // up neighbours in pair layout: lane l loads columns base + 2l, base + 2l + 1 (16 bytes)
-      const int64_t cpair = base + 2 * lane;
-      const int64_t* xc = X + min(cpair, nd - 2);  // out-of-range lanes load a valid pair, unused
+      const int64_t* xc = X + min(base + 2 * lane, nd - 2);  // out-of-range lanes load a valid pair, unused
       longlong2 u0 = make_longlong2(0, 0), u1 = make_longlong2(0, 0);
       for (int e = 0; e < nmax; e += 4) {
         if (e < n0) {
@@ -773,23 +776,23 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
       }
 #pragma unroll
       for (int half = 0; half < 2; ++half) {
-        const int64_t c = base + 32 * half + lane;
+        const int c = base + 32 * half + lane;
         if (c >= nd) continue;
         const longlong2 xo = xs2[c];
-        int64_t h0 = corr0 * xo.x + (half ? up_hi[0] : up_lo[0]);
-        int64_t h1 = corr1 * xo.y + (half ? up_hi[1] : up_lo[1]);
+        int64_t h0 = (int64_t)corr0 * xo.x + (half ? up_hi[0] : up_lo[0]);
+        int64_t h1 = (int64_t)corr1 * xo.y + (half ? up_hi[1] : up_lo[1]);
         // dn neighbours: two bonds per table word (byte offsets into xs2), + rows then - rows;
         // offset 16*nd reads zeros
         const uint32_t* tc = tab + c;
         for (int p = 0; p < np; ++p) {
-          const uint32_t w = tc[(int64_t)p * nd];
+          const uint32_t w = tc[p * nd];
           const longlong2 va = *(const longlong2*)((const char*)xs2 + (w & 0xffffu));
           const longlong2 vb = *(const longlong2*)((const char*)xs2 + (w >> 16));
           h0 += va.x + vb.x;
           h1 += va.y + vb.y;
         }
         for (int p = np; p < ne; ++p) {
-          const uint32_t w = tc[(int64_t)p * nd];
+          const uint32_t w = tc[p * nd];
           const longlong2 va = *(const longlong2*)((const char*)xs2 + (w & 0xffffu));
           const longlong2 vb = *(const longlong2*)((const char*)xs2 + (w >> 16));
           h0 -= va.x + vb.x;
@@ -800,13 +803,13 @@ __global__ void __launch_bounds__(MV3_MAXNT, 1)
         const int64_t ed64 = half ? e64_hi : e64_lo;
         {
           const int64_t w0 = (int64_t)a.t_int * h0 + bfp_diag_col<DIAG64>(a, eu0, ef0, su0, sd, ed32, ed64, xo.x);
-          st_stream(W + row0 * nd + c, w0, stream);
+          st_stream(W + (o0 + c), w0, stream);
           add128(dot, mul_s64(xo.x, w0));
           mx = max(mx, uabs64(w0));
         }
         if (nr > 1) {
           const int64_t w1 = (int64_t)a.t_int * h1 + bfp_diag_col<DIAG64>(a, eu1, ef1, su1, sd, ed32, ed64, xo.y);
-          st_stream(W + (row0 + 1) * nd + c, w1, stream);
+          st_stream(W + (o0 + nd + c), w1, stream);
           add128(dot, mul_s64(xo.y, w1));
           mx = max(mx, uabs64(w1));
         }
