@@ -14,7 +14,8 @@
 // address is obtained with cudaGetSymbolAddress (with the device current) and passed to the
 // kernel. That set-up happens in the first call on each device (and again after the device's
 // context was replaced, e.g. after cudaDeviceReset: the cache is keyed on the context), so
-// that first call should come before any stream capture on the device. Every call shares the
+// that first call should come before any stream capture on the device; later calls make no
+// call that a stream capture forbids and can be captured into a CUDA graph. Every call shares the
 // array: calls that overlap on the GPU (different streams without ordering) race on it. The
 // kernel rebuilds every scratch value it reads, so nothing has to be cleared between calls.
 #include <cuda.h>
@@ -64,9 +65,16 @@ static ed_status scratch_address(double** out) {
   int dev = 0;
   ED_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(ED_ERR_INVALID_ARG, "device index out of range");
-  ED_CUDA(cudaFree(nullptr));  // makes the device's primary context current on this thread
   void* ctx = nullptr;
   ED_TRY(current_context(&ctx));
+  if (!ctx) {
+    // no context on this thread yet: make the device's primary context current (only then:
+    // cudaFree is not allowed while a stream of the device is being captured, and a thread
+    // that captures already has its context current)
+    ED_CUDA(cudaFree(nullptr));
+    ED_TRY(current_context(&ctx));
+    if (!ctx) return fail(ED_ERR_CUDA, "no current context on the device");
+  }
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
   if (!g_scratch[dev].ptr || g_scratch[dev].ctx != ctx) {
     void* p = nullptr;

@@ -513,8 +513,10 @@ ED_API ed_status ed_plan_set_wait_limit(ed_plan plan, int64_t polls);
  * m <= 4096; larger m returns ED_ERR_INVALID_ARG, like ed_tridiag_lowest. The first call on a
  * device (and the first after its context was replaced, e.g. by cudaDeviceReset) looks up the
  * array's device address (cudaGetSymbolAddress); that call should come before any stream
- * capture on the device. All calls share the array: calls that overlap on the GPU race on it.
- * Calls no cudaMalloc / cudaFree and no allocating library routine. */
+ * capture on the device, and later calls can be captured into a CUDA graph. All calls share
+ * the array: calls that overlap on the GPU race on it. Calls no cudaMalloc and no allocating
+ * library routine; cudaFree(NULL), which frees nothing, only on a thread without a current
+ * context, to make the device's primary context current. */
 ED_API ed_status ed_tridiag_lowest_noalloc(const double* d_alpha, const double* d_beta, int m,
                                            double* d_value, double* d_vec, ed_stream_t stream);
 

@@ -121,3 +121,42 @@ def test_noalloc_in_fresh_process(cuda):
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "fresh-process no-alloc ok" in r.stdout
+
+
+def test_noalloc_in_cuda_graph(cuda):
+    """After a warm-up call, a call captured into a CUDA graph replays correctly with its
+    inputs changed in place between replays (the graph keeps the scratch address it was
+    captured with)."""
+    from cmpy_gb300 import _native as N
+
+    L = N.lib()
+    m = 1000  # above the shared-memory size: the kernel works in the static array
+    a_h, b_h = _problem(m, 11)
+    a, b = torch.as_tensor(a_h).cuda(), torch.as_tensor(b_h).cuda()
+    val = torch.empty(1, dtype=torch.float64, device="cuda")
+    vec = torch.empty(m, dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        st = L.ed_tridiag_lowest_noalloc(a.data_ptr(), b.data_ptr(), m, val.data_ptr(), vec.data_ptr(),
+                                         s.cuda_stream)
+        assert st == 0, L.ed_last_error().decode()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    status = []
+    with torch.cuda.graph(g):
+        cs = torch.cuda.current_stream().cuda_stream
+        status.append(L.ed_tridiag_lowest_noalloc(a.data_ptr(), b.data_ptr(), m, val.data_ptr(), vec.data_ptr(), cs))
+    assert status == [0], L.ed_last_error().decode()
+    for seed in (12, 13):
+        a2, b2 = _problem(m, seed)
+        a.copy_(torch.as_tensor(a2))
+        b.copy_(torch.as_tensor(b2))
+        g.replay()
+        torch.cuda.synchronize()
+        st, v_ref, x_ref = _call(L.ed_tridiag_lowest, a, b, True)
+        assert st == 0
+        torch.cuda.synchronize()
+        assert abs(val.item() - v_ref.item()) <= TOL * max(1.0, abs(v_ref.item()))
+        torch.testing.assert_close(vec, x_ref, rtol=0, atol=TOL)
+        e_sp, _ = _scipy_lowest(a2, b2)
+        assert abs(val.item() - e_sp) <= TOL * max(1.0, abs(e_sp))
