@@ -846,7 +846,7 @@ def run_reference(args, rank, world):
 
 
 def run_chain6():
-    """Config 1 (correctness configuration, time reported): 6-site open Hubbard chain, t=1,
+    """The small correctness workload, timed: 6-site open Hubbard chain, t=1,
     U=4, mu=2, sector (3,3): Lanczos ground state (tol 1e-12) and the T=0 Lehmann Green's
     function on site 0, spin up, at 512 real frequencies in [-8, 8] with eta = 0.05."""
     import torch
@@ -900,7 +900,7 @@ def cpu_baseline_heisenberg():
 
 
 def cpu_baseline_chain6():
-    """The reference's CPU path for config 1 (same model as run_chain6): dense sector
+    """The reference's CPU path for the 6-site chain workload (same model as run_chain6): dense sector
     Hamiltonians from its triplets, numpy.linalg.eigh of the (3,3) sector for the ground state
     and of the (4,3) and (2,3) sectors for the T=0 Lehmann sum at 512 frequencies
     (cmpy/exactdiag.py:46-57, 215-245), one host core."""
@@ -982,7 +982,7 @@ def main():
             out["cpu_baseline"] = None
         if not args.no_extras and world == 1:
             for key, fn in (("batched_sweep", run_batched_sweep), ("batched_disorder", run_disorder_batch),
-                            ("adjoint", run_adjoint), ("heisenberg20", run_heisenberg), ("chain6_config1", run_chain6),
+                            ("adjoint", run_adjoint), ("heisenberg20", run_heisenberg), ("chain6_gs_lehmann512", run_chain6),
                             ("matvec_f64_t07", run_f64_matvec)):
                 try:
                     out[key] = fn()
@@ -990,7 +990,7 @@ def main():
                     out[key] = {"error": f"{type(exc).__name__}: {exc}"}
             # the reference's CPU path beside the two small configurations (cpu_baseline leg)
             if not args.no_cpu_baseline:
-                for key, fn in (("heisenberg20", cpu_baseline_heisenberg), ("chain6_config1", cpu_baseline_chain6)):
+                for key, fn in (("heisenberg20", cpu_baseline_heisenberg), ("chain6_gs_lehmann512", cpu_baseline_chain6)):
                     if isinstance(out.get(key), dict) and "error" not in out[key]:
                         try:
                             out[key]["cpu_baseline"] = fn()
