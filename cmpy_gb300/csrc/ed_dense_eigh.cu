@@ -11,15 +11,17 @@
 //    order <= 1024 take every step in one CTA per matrix instead (block barriers between the
 //    phases: no launch per step). The rank-2 update is formed as v_i w_j + w_i v_j with
 //    separately rounded products, so A stays exactly symmetric.
-// 2. All eigenvalues of T by bisection on Sturm counts (one thread per eigenvalue), ascending.
+// 2. All eigenvalues of T by multisection on Sturm counts (a group of 1-32 lanes per
+//    eigenvalue, sized to fill the GPU), ascending.
 // 3. Eigenvectors of T by inverse iteration (Gaussian elimination with partial pivoting of
-//    T - lambda I, start vectors that differ per index), one thread per cluster of eigenvalues
-//    closer than 1e-7 max(1, |lambda|max): each iterate is re-orthogonalised against the
-//    cluster's earlier members, so degenerate sector eigenvalues (symmetries) give an
-//    orthonormal basis of the eigenspace.
+//    T - lambda I, start vectors that differ per index), one warp per cluster of eigenvalues
+//    closer than 1e-7 max(1, |lambda|max) with its work arrays in shared memory: each iterate
+//    is re-orthogonalised against the cluster's earlier members, so degenerate sector
+//    eigenvalues (symmetries) give an orthonormal basis of the eigenspace.
 // 4. Back-transformation y = Q z (one warp per eigenvector, reflectors in reverse order).
 // Output: eigenvalues ascending, eigenvector i as row i of Z (Z = V^T).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <vector>
 
@@ -211,6 +213,9 @@ __global__ void k_hh_finish(DenseBatch m, int B) {
   const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
   m.glim[2 * b] = lo - pad;
   m.glim[2 * b + 1] = hi + pad;
+  // P (free after the reduction): the squared couplings of the Sturm recurrence
+  double* bb = m.P + (size_t)b * m.nmax;
+  for (int i = 0; i < n; ++i) bb[i] = bt[i] * bt[i];
 }
 
 // a given tridiagonal (alpha[0..m), beta[1..m)) as T of a one-matrix batch, and its Gershgorin
@@ -229,25 +234,167 @@ __global__ void k_tri_setup(DenseBatch m, const double* alpha, const double* bet
   const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
   m.glim[0] = lo - pad;
   m.glim[1] = hi + pad;
+  for (int i = 0; i < n; ++i) m.P[i] = m.bet[i] * m.bet[i];
 }
 
-// eigenvalue i of T by bisection: the smallest x with at least i + 1 eigenvalues below
-__global__ void k_tri_eigvals(DenseBatch m, int B, double* W) {
-  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int b = (int)(g / m.nmax), i = (int)(g % m.nmax);
+// All eigenvalues of T by multisection: a group of P lanes (P a power of two <= 32) per
+// eigenvalue. Each round the group counts the eigenvalues below P equidistant interior points
+// of its bracket and keeps the gap where the count first reaches i + 1, so a bracket shrinks by
+// P + 1 per round (P = 1 is bisection). The launch picks P so that the batch fills the GPU: a
+// few eigenvalues take whole warps (fewer rounds of the latency-bound FP64 recurrence), many
+// take single lanes (the FP64 pipe's throughput is then the bound). A bracket stops when a
+// round makes no progress (its points round onto its ends); W = its midpoint, ascending in i.
+// bb: the squared couplings (m.P after k_hh_finish / k_tri_setup).
+__global__ void k_tri_eigvals_ms(DenseBatch m, int B, double* W, int P) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int gpw = 32 / P, grp = lane / P, j = lane - grp * P;
+  const int64_t e = gw * gpw + grp;  // eigenvalue slot over the batch (b, i)
+  const int b = (int)(e / m.nmax), i = (int)(e % m.nmax);
+  const int n = b < B ? m.n[b] : 0;
+  bool done = !(b < B && i < n);  // uniform within a group
+  const double* d = m.d + (size_t)(done ? 0 : b) * m.nmax;
+  const double* bt = m.bet + (size_t)(done ? 0 : b) * m.nmax;
+  const double* bb = m.P + (size_t)(done ? 0 : b) * m.nmax;
+  double lo = done ? 0.0 : m.glim[2 * b], hi = done ? 0.0 : m.glim[2 * b + 1];
+  const unsigned gmask = (P == 32) ? 0xffffffffu : (((1u << P) - 1u) << (grp * P));
+  const double den = 1.0 / (double)(P + 1);
+  for (int round = 0; round < 256; ++round) {
+    if (__all_sync(0xffffffffu, done)) break;
+    int cnt = 0;
+    if (!done) cnt = sturm_count(d, bt, bb, n, lo + (hi - lo) * ((double)(j + 1) * den));
+    const unsigned hit = __ballot_sync(0xffffffffu, !done && cnt >= i + 1) & gmask;
+    if (!done) {
+      const int t = hit ? (__ffs(hit) - 1 - grp * P) : P;  // first point with >= i + 1 below
+      const double nlo = (t == 0) ? lo : lo + (hi - lo) * ((double)t * den);
+      const double nhi = (t == P) ? hi : lo + (hi - lo) * ((double)(t + 1) * den);
+      if (!(nlo > lo) && !(nhi < hi)) done = true;  // the points rounded onto the ends
+      lo = nlo;
+      hi = nhi;
+    }
+  }
+  if (b < B && i < n && j == 0) W[(size_t)b * m.nmax + i] = 0.5 * (lo + hi);
+}
+
+// bytes of shared memory k_tri_eigvecs_warp takes for order n
+__host__ __device__ inline size_t eigvec_smem(int n) { return (size_t)5 * n * sizeof(double) + (((size_t)n + 15) & ~(size_t)15); }
+
+// The eigenvectors of T by inverse iteration as in k_tri_eigvecs, one warp (one block) per
+// cluster of eigenvalues, with the elimination's work arrays and the iterate in shared memory
+// (eigvec_smem(n) bytes): lane 0 runs the sequential elimination and the two triangular
+// solves, the whole warp the start vector, the scaling, the re-orthogonalisation against the
+// cluster's earlier members and the normalisation. Same clusters, same steps.
+__global__ void __launch_bounds__(32) k_tri_eigvecs_warp(DenseBatch m, int B, const double* W, double* Z,
+                                                         int64_t ldz, int64_t sz) {
+  extern __shared__ __align__(16) double ws[];
+  const int lane = threadIdx.x;
+  const int64_t e = blockIdx.x;
+  const int b = (int)(e / m.nmax), i0 = (int)(e % m.nmax);
   if (b >= B) return;
   const int n = m.n[b];
-  if (i >= n) return;
-  const double* d = m.d + (size_t)b * m.nmax;
+  if (i0 >= n) return;
+  const double* w = W + (size_t)b * m.nmax;
+  const double ctol = 1e-7 * fmax(1.0, fmax(fabs(w[0]), fabs(w[n - 1])));
+  if (i0 > 0 && w[i0] - w[i0 - 1] <= ctol) return;  // not the first member of its cluster
+  int i1 = i0 + 1;
+  while (i1 < n && w[i1] - w[i1 - 1] <= ctol) ++i1;
+  const double* a = m.d + (size_t)b * m.nmax;
   const double* bt = m.bet + (size_t)b * m.nmax;
-  double lo = m.glim[2 * b], hi = m.glim[2 * b + 1];
-  for (int it = 0; it < 200; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (mid <= lo || mid >= hi) break;
-    if (sturm_count(d, bt, nullptr, n, mid) >= i + 1) hi = mid;
-    else lo = mid;
+  double* Zb = Z + (size_t)b * sz;
+  double* dd = ws;
+  double* du = ws + n;
+  double* du2 = ws + 2 * n;
+  double* ml = ws + 3 * n;
+  double* vec = ws + 4 * n;
+  unsigned char* pv = (unsigned char*)(ws + 5 * n);  // 1 if rows r and r + 1 were swapped
+  for (int q = i0; q < i1; ++q) {
+    const double ev = w[q];
+    const double tiny = 1e-300 + 1e-18 * fmax(fabs(ev), 1.0);
+    // start vector in [0.5, 1.5), a hash of (q, r): differs with the index
+    for (int r = lane; r < n; r += 32) {
+      uint32_t h = 2654435761u * (uint32_t)(q + 1) ^ (2246822519u * (uint32_t)(r + 1));
+      h ^= h >> 15;
+      h *= 2246822519u;
+      h ^= h >> 13;
+      vec[r] = 0.5 + (double)(h & 0xffffu) / 65536.0;
+      dd[r] = a[r] - ev;
+      du[r] = (r + 1 < n) ? bt[r + 1] : 0.0;
+      du2[r] = 0.0;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      for (int r = 0; r < n - 1; ++r) {
+        const double sub = bt[r + 1];
+        if (fabs(dd[r]) >= fabs(sub)) {
+          pv[r] = 0;
+          if (dd[r] == 0.0) dd[r] = tiny;
+          const double rc = 1.0 / dd[r];
+          const double l = sub * rc;
+          ml[r] = l;
+          dd[r + 1] -= l * du[r];
+          dd[r] = rc;
+        } else {
+          pv[r] = 1;
+          const double rc = 1.0 / sub;
+          const double l = dd[r] * rc;
+          ml[r] = l;
+          const double t0 = dd[r + 1], t1 = (r + 2 < n) ? du[r + 1] : 0.0, odu = du[r];
+          du[r] = t0;
+          du2[r] = t1;
+          dd[r + 1] = odu - l * t0;
+          if (r + 2 < n) du[r + 1] = -l * t1;
+          dd[r] = rc;
+        }
+      }
+      if (dd[n - 1] == 0.0) dd[n - 1] = tiny;
+      dd[n - 1] = 1.0 / dd[n - 1];
+    }
+    __syncwarp();
+    for (int it = 0; it < 3; ++it) {
+      if (lane == 0) {
+        for (int r = 0; r < n - 1; ++r) {
+          if (pv[r]) {
+            const double t = vec[r];
+            vec[r] = vec[r + 1];
+            vec[r + 1] = t - ml[r] * vec[r];
+          } else {
+            vec[r + 1] -= ml[r] * vec[r];
+          }
+        }
+        for (int r = n - 1; r >= 0; --r) {
+          double sacc = vec[r];
+          if (r + 1 < n) sacc -= du[r] * vec[r + 1];
+          if (r + 2 < n) sacc -= du2[r] * vec[r + 2];
+          vec[r] = sacc * dd[r];
+        }
+      }
+      __syncwarp();
+      double mx = 0.0;
+      for (int r = lane; r < n; r += 32) mx = fmax(mx, fabs(vec[r]));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      const double sc = mx > 0.0 ? 1.0 / mx : 1.0;  // keep the iterate in range
+      for (int r = lane; r < n; r += 32) vec[r] *= sc;
+      __syncwarp();
+      for (int pass = 0; pass < 2; ++pass)
+        for (int l = i0; l < q; ++l) {
+          const double* zl = Zb + (size_t)l * ldz;
+          double sp = 0.0;
+          for (int r = lane; r < n; r += 32) sp = fma(zl[r], vec[r], sp);
+          sp = warp_sum_d(sp);
+          for (int r = lane; r < n; r += 32) vec[r] = fma(-sp, zl[r], vec[r]);
+          __syncwarp();
+        }
+      double nrm = 0.0;
+      for (int r = lane; r < n; r += 32) nrm = fma(vec[r], vec[r], nrm);
+      nrm = 1.0 / sqrt(warp_sum_d(nrm));
+      for (int r = lane; r < n; r += 32) vec[r] *= nrm;
+      __syncwarp();
+    }
+    double* zq = Zb + (size_t)q * ldz;
+    for (int r = lane; r < n; r += 32) zq[r] = vec[r];
+    __syncwarp();
   }
-  W[(size_t)b * m.nmax + i] = 0.5 * (lo + hi);
 }
 
 // The eigenvectors of T by inverse iteration, one thread per cluster of eigenvalues (values
@@ -376,6 +523,48 @@ __global__ void __launch_bounds__(DE_NT) k_hh_back(DenseBatch m, int B, double* 
   }
 }
 
+// lanes per eigenvalue of k_tri_eigvals_ms for E eigenvalues on a GPU with `sms` SMs: the
+// largest power of two <= 32 that keeps the launch near four warps per SM
+static int eigvals_lanes(int64_t E, int sms) {
+  int P = 1;
+  while (P < 32 && E * (int64_t)(2 * P) <= (int64_t)sms * 4 * 32) P *= 2;
+  return P;
+}
+
+// eigenvalues (ascending) and eigenvectors of the B tridiagonals of m (d, bet, glim and the
+// squared couplings in P set) into W [B][nmax] and Z (row i = eigenvector i). The eigenvectors
+// take the shared-memory kernel when its arrays fit in one CTA's shared memory, else the
+// kernel with global work arrays (5 nmax^2 doubles per matrix, allocated here).
+static ed_status tridiag_eigenpairs(const DeviceContext* ctx, DenseBatch m, int B, double* W, double* Z, int64_t ldz,
+                                    int64_t sz, cudaStream_t s) {
+  const int64_t E = (int64_t)B * m.nmax;
+  const int P = eigvals_lanes(E, ctx->num_sms);
+  const int64_t warps = (E + (32 / P) - 1) / (32 / P);
+  k_tri_eigvals_ms<<<(int)((warps + 3) / 4), 128, 0, s>>>(m, B, W, P);
+  ED_CHECK_LAUNCH("k_tri_eigvals_ms");
+  const size_t sm = eigvec_smem(m.nmax);
+  if (sm + 1024 <= (size_t)ctx->smem_optin) {
+    static std::atomic<uint64_t> done{0};
+    const uint64_t bit = 1ull << (ctx->device & 63);
+    if (sm > 48 * 1024 && !(done.load() & bit)) {
+      ED_CUDA(cudaFuncSetAttribute(k_tri_eigvecs_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   ctx->smem_optin - 1024));
+      done.fetch_or(bit);
+    }
+    k_tri_eigvecs_warp<<<(unsigned)E, 32, sm, s>>>(m, B, W, Z, ldz, sz);
+    ED_CHECK_LAUNCH("k_tri_eigvecs_warp");
+    return ED_OK;
+  }
+  double* work = nullptr;
+  ED_CUDA(cudaMallocAsync((void**)&work, (size_t)5 * E * m.nmax * sizeof(double), s));
+  k_tri_eigvecs<<<(int)((E + 31) / 32), 32, 0, s>>>(m, B, W, Z, ldz, sz, work);
+  const cudaError_t e = cudaGetLastError();
+  count_launches(1);
+  ED_CUDA(cudaFreeAsync(work, s));
+  if (e != cudaSuccess) return cuda_fail(e, "k_tri_eigvecs");
+  return ED_OK;
+}
+
 }  // namespace ed
 
 using namespace ed;
@@ -396,8 +585,8 @@ ED_API ed_status ed_dense_eigh_batch(double* d_a, int64_t lda, int64_t stride_a,
   const size_t nm = (size_t)B * n_max;
   double* buf = nullptr;
   int* dn = nullptr;
-  // d, bet, tau, P (4 nm), Gershgorin (2 B), inverse-iteration work (5 nm n_max)
-  ED_CUDA(cudaMallocAsync((void**)&buf, (4 * nm + 2 * (size_t)B + 5 * nm * (size_t)n_max) * sizeof(double), s));
+  // d, bet, tau, P (4 nm), Gershgorin (2 B)
+  ED_CUDA(cudaMallocAsync((void**)&buf, (4 * nm + 2 * (size_t)B) * sizeof(double), s));
   ED_CUDA(cudaMallocAsync((void**)&dn, (size_t)B * sizeof(int), s));
   ED_CUDA(cudaMemcpyAsync(dn, h_n, (size_t)B * sizeof(int), cudaMemcpyHostToDevice, s));
   DenseBatch m;
@@ -411,7 +600,6 @@ ED_API ed_status ed_dense_eigh_batch(double* d_a, int64_t lda, int64_t stride_a,
   m.P = buf + 3 * nm;
   m.glim = buf + 4 * nm;
   m.nmax = n_max;
-  double* work = buf + 4 * nm + 2 * (size_t)B;
   ed_status st = ED_OK;
   const int rows_per = DE_NT / 32;
   if (n_max <= DE_SMALL) {
@@ -433,16 +621,17 @@ ED_API ed_status ed_dense_eigh_batch(double* d_a, int64_t lda, int64_t stride_a,
   }
   if (st == ED_OK) {
     k_hh_finish<<<(B + 127) / 128, 128, 0, s>>>(m, B);
-    // one thread per eigenvalue in blocks of one warp: the bisections and inverse iterations
-    // are FP64 chains, so they are spread over as many SMs' FP64 pipes as possible
+    const cudaError_t e = cudaGetLastError();
+    count_launches(1);
+    if (e != cudaSuccess) st = cuda_fail(e, "k_hh_finish");
+  }
+  if (st == ED_OK) st = tridiag_eigenpairs(ctx, m, B, d_w, d_z, ldz, stride_z, s);
+  if (st == ED_OK) {
     const int64_t nt = (int64_t)B * n_max;
-    const int g1 = (int)((nt + 31) / 32);
-    k_tri_eigvals<<<g1, 32, 0, s>>>(m, B, d_w);
-    k_tri_eigvecs<<<g1, 32, 0, s>>>(m, B, d_w, d_z, ldz, stride_z, work);
     k_hh_back<<<(int)((nt * 32 + DE_NT - 1) / DE_NT), DE_NT, 0, s>>>(m, B, d_z, ldz, stride_z);
     const cudaError_t e = cudaGetLastError();
-    count_launches(4);
-    if (e != cudaSuccess) st = cuda_fail(e, "tridiagonal eigenpairs");
+    count_launches(1);
+    if (e != cudaSuccess) st = cuda_fail(e, "k_hh_back");
   }
   cudaFreeAsync(buf, s);
   cudaFreeAsync(dn, s);
@@ -459,7 +648,7 @@ ED_API ed_status ed_tridiag_eigh(const double* d_alpha, const double* d_beta, in
   cudaStream_t s = as_stream(stream);
   double* buf = nullptr;
   int* dn = nullptr;
-  ED_CUDA(cudaMallocAsync((void**)&buf, (4 * (size_t)m + 2 + 5 * (size_t)m * m) * sizeof(double), s));
+  ED_CUDA(cudaMallocAsync((void**)&buf, (4 * (size_t)m + 2) * sizeof(double), s));
   ED_CUDA(cudaMallocAsync((void**)&dn, sizeof(int), s));
   ED_CUDA(cudaMemcpyAsync(dn, &m, sizeof(int), cudaMemcpyHostToDevice, s));
   DenseBatch b{};
@@ -470,16 +659,14 @@ ED_API ed_status ed_tridiag_eigh(const double* d_alpha, const double* d_beta, in
   b.P = buf + 3 * (size_t)m;
   b.glim = buf + 4 * (size_t)m;
   b.nmax = m;
-  const int g1 = (m + 31) / 32;
   k_tri_setup<<<1, 1, 0, s>>>(b, d_alpha, d_beta, m);
-  k_tri_eigvals<<<g1, 32, 0, s>>>(b, 1, d_w);
-  k_tri_eigvecs<<<g1, 32, 0, s>>>(b, 1, d_w, d_z, ldz, (int64_t)m * ldz, buf + 4 * (size_t)m + 2);
   const cudaError_t e = cudaGetLastError();
-  count_launches(3);
+  count_launches(1);
+  ed_status st = e != cudaSuccess ? cuda_fail(e, "k_tri_setup") : ED_OK;
+  if (st == ED_OK) st = tridiag_eigenpairs(ctx, b, 1, d_w, d_z, ldz, (int64_t)m * ldz, s);
   cudaFreeAsync(buf, s);
   cudaFreeAsync(dn, s);
-  if (e != cudaSuccess) return cuda_fail(e, "tridiagonal eigenpairs");
-  return ED_OK;
+  return st;
 }
 
 }  // extern "C"

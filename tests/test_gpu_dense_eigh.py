@@ -131,3 +131,30 @@ def test_invalid_arguments(cuda):
     hn = (C.c_int * 1)(5)  # order above n_max
     st = N.lib().ed_dense_eigh_batch(N.ptr(a), 4, 16, hn, 1, 4, N.ptr(w), N.ptr(a), 4, 16, None)
     assert st == N.ED_ERR_INVALID_ARG
+
+
+def test_tridiagonal_beyond_shared_memory(cuda):
+    """m = 6000: the inverse-iteration arrays (5 m doubles) no longer fit in one CTA's shared
+    memory, so the eigenvectors take the kernel with global work arrays; eigenvalues and
+    eigenpair residuals against LAPACK."""
+    from cmpy_gb300 import engine as E
+
+    m = 6000
+    rng = np.random.default_rng(6000)
+    a = rng.standard_normal(m)
+    b = np.concatenate([[0.0], rng.standard_normal(m - 1)])
+    w, V = E.tridiag_eigh(torch.as_tensor(a).cuda(), torch.as_tensor(b).cuda())
+    w, V = w.cpu().numpy(), V.cpu().numpy()
+    w_ref = sla.eigh_tridiagonal(a, b[1:], eigvals_only=True)
+    scale = np.max(np.abs(w_ref))
+    np.testing.assert_allclose(w, w_ref, rtol=0, atol=TOL_W * scale)
+    TV = a[:, None] * V
+    TV[:-1] += b[1:, None] * V[1:]
+    TV[1:] += b[1:, None] * V[:-1]
+    assert np.max(np.abs(TV - V * w)) <= TOL_V * scale
+    # orthogonality of 200 random eigenvectors: pairs closer than the cluster tolerance are
+    # re-orthogonalised; for close pairs above it inverse iteration's orthogonality error is
+    # ~ eps ||T|| / gap (smallest gaps ~1e-7 among 6000 values), hence 1e-8
+    cols = rng.choice(m, 200, replace=False)
+    G = V[:, cols].T @ V[:, cols]
+    assert np.max(np.abs(G - np.eye(len(cols)))) <= 1e-8
