@@ -25,10 +25,14 @@
 #include <cmath>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "ed_common.cuh"
 #include "ed_tridiag.cuh"
 
 namespace ed {
+
+namespace cg = cooperative_groups;
 
 constexpr int DE_NT = 256;
 
@@ -124,11 +128,99 @@ __global__ void __launch_bounds__(DE_NT) k_hh_update(DenseBatch m, int k) {
     ai[j] = __dsub_rn(ai[j], __dadd_rn(__dmul_rn(vi, w[j]), __dmul_rn(wi, v[j])));
 }
 
+// All Householder steps of one matrix per thread-block cluster of CS CTAs (one per SM), for
+// orders where per-step launches cost more than the FP64 work they spread: the matrix stays in
+// global memory (L2-resident at these orders) and the phases of a step are separated by
+// cluster barriers instead of launches. Row i > k of step k belongs to warp (i - k - 1) mod NW
+// of the cluster (NW = 8 CS warps) for both the product p = tau A22 v and the rank-2 update.
+// Each p_i is written into the shared memory of every CTA of the cluster (distributed shared
+// memory), so after the barrier every CTA forms w = p - (tau/2)(p.v) v from local copies. The
+// warp that owns row k + 1 (warp 0 of rank 0) forms reflector k + 1 as soon as it has updated
+// that row, while the other rows are still being updated. A step takes two cluster barriers.
+// Shared memory: p and w, 2 n_max doubles. Same arithmetic as the per-step kernels, except
+// that the norm of the reflector row and the dot p.v are summed in another order.
+template <int CS>
+__global__ void __launch_bounds__(DE_NT) k_hh_cluster(DenseBatch m) {
+  extern __shared__ double hsm[];
+  __shared__ double red[DE_NT / 32];
+  __shared__ double kk_s;
+  cg::cluster_group cl = cg::this_cluster();
+  const int b = blockIdx.y, n = m.n[b];
+  double* ps = hsm;           // p, written by every CTA of the cluster
+  double* ws = hsm + m.nmax;  // w
+  const int rank = (int)cl.block_rank();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gw = rank * (DE_NT / 32) + warp, NW = CS * (DE_NT / 32);
+  double* Ab = m.A + (size_t)b * m.sa;
+  double* tau = m.tau + (size_t)b * m.nmax;
+  // reflector of row k (warp 0 of rank 0), as k_hh_column
+  auto reflector = [&](int k) {
+    double* row = Ab + (size_t)k * m.lda;
+    double sq = 0.0;
+    for (int i = k + 2 + lane; i < n; i += 32) sq = fma(row[i], row[i], sq);
+    sq = warp_sum_d(sq);
+    if (lane == 0) {
+      const double x0 = row[k + 1];
+      double t = 0.0, alpha = x0;
+      if (sq > 0.0) {
+        const double nrm = sqrt(fma(x0, x0, sq));
+        alpha = x0 >= 0.0 ? -nrm : nrm;
+        const double v0 = x0 - alpha;
+        t = 2.0 / fma(v0, v0, sq);
+        row[k + 1] = v0;
+      }
+      tau[k] = t;
+      m.d[(size_t)b * m.nmax + k] = row[k];
+      m.bet[(size_t)b * m.nmax + k + 1] = alpha;
+    }
+    __syncwarp();
+  };
+  if (n >= 3 && rank == 0 && warp == 0) reflector(0);
+  cl.sync();
+  for (int k = 0; k + 3 <= n; ++k) {
+    const double t = tau[k];
+    const double* v = Ab + (size_t)k * m.lda;
+    // p_i = t sum_{j>k} A[i][j] v_j, one warp per row, into every CTA's copy of p
+    for (int i = k + 1 + gw; i < n; i += NW) {
+      const double* ai = Ab + (size_t)i * m.lda;
+      double sp = 0.0;
+      for (int j = k + 1 + lane; j < n; j += 32) sp = fma(ai[j], v[j], sp);
+      sp = warp_sum_d(sp);
+      if (lane < CS) *cl.map_shared_rank(ps + i, lane) = t * sp;
+    }
+    cl.sync();
+    // w = p - (t/2)(p.v) v from the local copy of p
+    double sd = 0.0;
+    for (int i = k + 1 + threadIdx.x; i < n; i += DE_NT) sd = fma(ps[i], v[i], sd);
+    sd = block_sum<DE_NT>(sd, red);
+    if (threadIdx.x == 0) kk_s = 0.5 * t * sd;
+    __syncthreads();
+    const double kk = kk_s;
+    for (int i = k + 1 + threadIdx.x; i < n; i += DE_NT) ws[i] = fma(-kk, v[i], ps[i]);
+    __syncthreads();
+    // A[i][j] -= v_i w_j + w_i v_j for i, j > k (products rounded separately: symmetric)
+    for (int i = k + 1 + gw; i < n; i += NW) {
+      if (t != 0.0) {
+        double* ai = Ab + (size_t)i * m.lda;
+        const double vi = v[i], wi = ws[i];
+        for (int j = k + 1 + lane; j < n; j += 32)
+          ai[j] = __dsub_rn(ai[j], __dadd_rn(__dmul_rn(vi, ws[j]), __dmul_rn(wi, v[j])));
+      }
+      if (i == k + 1 && k + 4 <= n) {  // warp 0 of rank 0: row k + 1 is final for this step
+        __syncwarp();
+        reflector(k + 1);
+      }
+    }
+    cl.sync();
+  }
+}
+
 // All Householder steps of one matrix per CTA (matrices of order <= DE_SMALL): the four phases
 // of a step separated by block barriers instead of launches. One SM's FP64 pipe does the
 // O(n^3) work, so this pays only for small orders: at n = 128 about 0.2 ms against ~1.5 ms of
 // per-step launches; at n = 300 the per-step launches over every SM are faster.
 constexpr int DE_SMALL = 128;
+constexpr int DE_CLUSTER_MAX = 640;  // largest order reduced by one cluster per matrix when the batch is small
 constexpr int DE_NTS = 1024;
 __global__ void __launch_bounds__(DE_NTS) k_hh_small(DenseBatch m) {
   __shared__ double sm[DE_NTS / 32];
@@ -523,6 +615,50 @@ __global__ void __launch_bounds__(DE_NT) k_hh_back(DenseBatch m, int B, double* 
   }
 }
 
+// Householder reduction of the batch by one cluster of CS CTAs per matrix; false when the
+// device cannot co-schedule such a cluster (the caller then launches per step)
+template <int CS>
+static bool hh_cluster_launch(const DeviceContext* ctx, DenseBatch m, int B, cudaStream_t s, ed_status* st) {
+  static std::atomic<uint64_t> done{0}, usable{0};
+  const uint64_t bit = 1ull << (ctx->device & 63);
+  const size_t smem = (size_t)2 * m.nmax * sizeof(double);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CS, B);
+  cfg.blockDim = dim3(DE_NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (!(done.load() & bit)) {
+    bool ok = true;
+    if (CS > 8)
+      ok = cudaFuncSetAttribute(k_hh_cluster<CS>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+    if (ok)
+      ok = cudaFuncSetAttribute(k_hh_cluster<CS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                ctx->smem_optin - 1024) == cudaSuccess;
+    int nc = 0;
+    if (ok) {
+      cudaLaunchConfig_t probe = cfg;
+      probe.gridDim = dim3(CS, 1);
+      probe.dynamicSmemBytes = 48 * 1024;
+      ok = cudaOccupancyMaxActiveClusters(&nc, k_hh_cluster<CS>, &probe) == cudaSuccess && nc >= 1;
+    }
+    (void)cudaGetLastError();
+    if (ok) usable.fetch_or(bit);
+    done.fetch_or(bit);
+  }
+  if (!(usable.load() & bit) || smem > 48 * 1024) return false;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, k_hh_cluster<CS>, m);
+  count_launches(1);
+  *st = e == cudaSuccess ? ED_OK : cuda_fail(e, "k_hh_cluster");
+  return true;
+}
+
 // lanes per eigenvalue of k_tri_eigvals_ms for E eigenvalues on a GPU with `sms` SMs: the
 // largest power of two <= 32 that keeps the launch near four warps per SM
 static int eigvals_lanes(int64_t E, int sms) {
@@ -609,7 +745,13 @@ ED_API ed_status ed_dense_eigh_batch(double* d_a, int64_t lda, int64_t stride_a,
     count_launches(1);
     if (e != cudaSuccess) st = cuda_fail(e, "Householder (one CTA per matrix)");
   }
-  for (int k = 0; n_max > DE_SMALL && k + 3 <= n_max && st == ED_OK; ++k) {
+  // orders above DE_SMALL: one cluster of 16 (else 8) CTAs per matrix while the clusters'
+  // SMs do the FP64 work faster than per-step launches over every SM would (order <= 640, or a
+  // batch that occupies the GPU with clusters); else four launches per step
+  bool stepped = n_max <= DE_SMALL;
+  if (!stepped && (n_max <= DE_CLUSTER_MAX || (int64_t)B * 16 >= ctx->num_sms))
+    stepped = hh_cluster_launch<16>(ctx, m, B, s, &st) || hh_cluster_launch<8>(ctx, m, B, s, &st);
+  for (int k = 0; !stepped && k + 3 <= n_max && st == ED_OK; ++k) {
     const int rem = n_max - k - 1;
     k_hh_column<<<B, DE_NT, 0, s>>>(m, k);
     k_hh_matvec<<<dim3((rem + rows_per - 1) / rows_per, B), DE_NT, 0, s>>>(m, k);
