@@ -165,7 +165,18 @@ def case_gs14(steps: int = 250) -> None:
     print(json.dumps({"case": "gs14", "steps": r.steps, "energy": r.energy}))
 
 
-PROFILE_CASES = {"gf14": case_gf14, "adjoint64": case_adjoint64, "sweep10": case_sweep10, "gs14": case_gs14}
+def case_chain6() -> None:
+    """The 6-site open chain workload (U=4, mu=2, t=1): ground state of (3,3) and the T=0
+    Lehmann G at 512 frequencies, whose dense eigenpairs of the (4,3) and (2,3) sectors (order
+    300 each, one batch) are the dense eigensolver's kernels; three times (the first warms
+    the plans)."""
+    for _ in range(3):
+        out = run_chain6()
+    print(json.dumps({"case": "chain6", "ms": out["ms"], "energy": out["gs_energy"]}))
+
+
+PROFILE_CASES = {"gf14": case_gf14, "adjoint64": case_adjoint64, "sweep10": case_sweep10, "gs14": case_gs14,
+                 "chain6": case_chain6}
 
 
 def peaks():
