@@ -283,31 +283,50 @@ __global__ void __launch_bounds__(DE_NTS) k_hh_small(DenseBatch m) {
 }
 
 // the last diagonal entries and the Gershgorin bounds of T (one thread per matrix)
-__global__ void k_hh_finish(DenseBatch m, int B) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+// the last two entries of T, its Gershgorin bounds and the squared couplings (P is free after
+// the reduction), one 128-thread block per matrix
+__global__ void __launch_bounds__(128) k_hh_finish(DenseBatch m, int B) {
+  __shared__ double slo[4], shi[4];
+  const int b = blockIdx.x;
   if (b >= B) return;
   const int n = m.n[b];
   const double* Ab = m.A + (size_t)b * m.sa;
   double* d = m.d + (size_t)b * m.nmax;
   double* bt = m.bet + (size_t)b * m.nmax;
-  bt[0] = 0.0;
-  if (n >= 2) {
-    d[n - 2] = Ab[(size_t)(n - 2) * m.lda + n - 2];
-    bt[n - 1] = Ab[(size_t)(n - 2) * m.lda + n - 1];
+  if (threadIdx.x == 0) {
+    bt[0] = 0.0;
+    if (n >= 2) {
+      d[n - 2] = Ab[(size_t)(n - 2) * m.lda + n - 2];
+      bt[n - 1] = Ab[(size_t)(n - 2) * m.lda + n - 1];
+    }
+    d[n - 1] = Ab[(size_t)(n - 1) * m.lda + n - 1];
   }
-  d[n - 1] = Ab[(size_t)(n - 1) * m.lda + n - 1];
+  __syncthreads();
   double lo = d[0], hi = d[0];
-  for (int i = 0; i < n; ++i) {
+  double* bb = m.P + (size_t)b * m.nmax;
+  for (int i = threadIdx.x; i < n; i += 128) {
     const double r = (i > 0 ? fabs(bt[i]) : 0.0) + (i + 1 < n ? fabs(bt[i + 1]) : 0.0);
     lo = fmin(lo, d[i] - r);
     hi = fmax(hi, d[i] + r);
+    bb[i] = bt[i] * bt[i];
   }
-  const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
-  m.glim[2 * b] = lo - pad;
-  m.glim[2 * b + 1] = hi + pad;
-  // P (free after the reduction): the squared couplings of the Sturm recurrence
-  double* bb = m.P + (size_t)b * m.nmax;
-  for (int i = 0; i < n; ++i) bb[i] = bt[i] * bt[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    slo[threadIdx.x >> 5] = lo;
+    shi[threadIdx.x >> 5] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    lo = fmin(fmin(slo[0], slo[1]), fmin(slo[2], slo[3]));
+    hi = fmax(fmax(shi[0], shi[1]), fmax(shi[2], shi[3]));
+    const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
+    m.glim[2 * b] = lo - pad;
+    m.glim[2 * b + 1] = hi + pad;
+  }
 }
 
 // a given tridiagonal (alpha[0..m), beta[1..m)) as T of a one-matrix batch, and its Gershgorin
@@ -762,7 +781,7 @@ ED_API ed_status ed_dense_eigh_batch(double* d_a, int64_t lda, int64_t stride_a,
     if (e != cudaSuccess) st = cuda_fail(e, "Householder step");
   }
   if (st == ED_OK) {
-    k_hh_finish<<<(B + 127) / 128, 128, 0, s>>>(m, B);
+    k_hh_finish<<<B, 128, 0, s>>>(m, B);
     const cudaError_t e = cudaGetLastError();
     count_launches(1);
     if (e != cudaSuccess) st = cuda_fail(e, "k_hh_finish");
