@@ -541,7 +541,7 @@ def tridiag_lowest_batch(alpha: torch.Tensor, beta: torch.Tensor, m) -> tuple[to
 def dense_eigh_batch(mats) -> list[tuple[torch.Tensor, torch.Tensor]]:
     """Every eigenpair of each real symmetric matrix in `mats` (square tensors), one call for
     the batch: [(eigenvalues ascending [n], eigenvectors as columns [n, n])] on the device.
-    The hand-written FP64 solver (Householder, Sturm bisection, inverse iteration)."""
+    The hand-written FP64 solver (Householder, Sturm multisection, inverse iteration)."""
     ms = [_as_dev_f64(a) for a in mats]
     if not ms:
         return []

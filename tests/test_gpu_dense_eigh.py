@@ -1,5 +1,5 @@
 """GPU parity of the library's dense symmetric eigensolver (ed_dense_eigh_batch: Householder
-tridiagonalisation, Sturm bisection, inverse iteration re-orthogonalised within clusters,
+tridiagonalisation, Sturm multisection, inverse iteration re-orthogonalised within clusters,
 back-transformation) and of the tridiagonal one (ed_tridiag_eigh), against numpy / scipy
 (LAPACK) on the CPU.
 
