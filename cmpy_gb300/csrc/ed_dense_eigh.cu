@@ -4,13 +4,15 @@
 //
 // For every matrix of the batch (order n_b <= n_max, row-major, overwritten):
 // 1. Householder tridiagonalisation A = Q T Q^T. Step k takes the reflector of row k beyond
-//    the diagonal, p = tau A22 v, w = p - (tau/2)(p.v) v, A22 -= v w^T + w v^T. Each step is
-//    four launches over the whole batch (reflector, matrix-vector product with one warp per row,
-//    the dot product, rank-2 update), so a single large matrix uses every SM; the FP64 pipe of
-//    this GPU (two FMAs per clock per SM) bounds the O(n^3) parts. Batches of matrices of
-//    order <= 1024 take every step in one CTA per matrix instead (block barriers between the
-//    phases: no launch per step). The rank-2 update is formed as v_i w_j + w_i v_j with
-//    separately rounded products, so A stays exactly symmetric.
+//    the diagonal, p = tau A22 v, w = p - (tau/2)(p.v) v, A22 -= v w^T + w v^T; the FP64 pipe
+//    of this GPU (two FMAs per clock per SM) and the latency of its dependent FP64 chains bound
+//    the O(n^3) parts. Three forms: orders <= 128 take every step in one CTA per matrix (block
+//    barriers between the phases); orders <= 640, or batches that fill the GPU with clusters,
+//    one thread-block cluster of 16 (else 8) CTAs per matrix (cluster barriers, p broadcast
+//    through distributed shared memory); larger orders four launches per step over the whole
+//    batch (reflector, matrix-vector product with one warp per row, the dot product, rank-2
+//    update), so a single large matrix uses every SM. The rank-2 update is formed as
+//    v_i w_j + w_i v_j with separately rounded products, so A stays exactly symmetric.
 // 2. All eigenvalues of T by multisection on Sturm counts (a group of 1-32 lanes per
 //    eigenvalue, sized to fill the GPU), ascending.
 // 3. Eigenvectors of T by inverse iteration (Gaussian elimination with partial pivoting of
