@@ -24,6 +24,7 @@
 // Output: eigenvalues ascending, eigenvector i as row i of Z (Z = V^T).
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cmath>
 #include <vector>
 
@@ -769,9 +770,20 @@ ED_API ed_status ed_dense_eigh_batch(double* d_a, int64_t lda, int64_t stride_a,
   // orders above DE_SMALL: one cluster of 16 (else 8) CTAs per matrix while the clusters'
   // SMs do the FP64 work faster than per-step launches over every SM would (order <= 640, or a
   // batch that occupies the GPU with clusters); else four launches per step
+  // CMPY_ED_HH_CLUSTER=16, 8 or 0 forces that cluster size or the per-step launches (for tests
+  // and comparisons; read once per process)
+  static int env_cluster = -2;
+  if (env_cluster == -2) {
+    const char* e = getenv("CMPY_ED_HH_CLUSTER");
+    env_cluster = e ? atoi(e) : -1;
+  }
   bool stepped = n_max <= DE_SMALL;
-  if (!stepped && (n_max <= DE_CLUSTER_MAX || (int64_t)B * 16 >= ctx->num_sms))
-    stepped = hh_cluster_launch<16>(ctx, m, B, s, &st) || hh_cluster_launch<8>(ctx, m, B, s, &st);
+  const bool want = env_cluster >= 0 ? env_cluster > 0
+                                     : (n_max <= DE_CLUSTER_MAX || (int64_t)B * 16 >= ctx->num_sms);
+  if (!stepped && want) {
+    if (env_cluster != 8) stepped = hh_cluster_launch<16>(ctx, m, B, s, &st);
+    if (!stepped) stepped = hh_cluster_launch<8>(ctx, m, B, s, &st);
+  }
   for (int k = 0; !stepped && k + 3 <= n_max && st == ED_OK; ++k) {
     const int rem = n_max - k - 1;
     k_hh_column<<<B, DE_NT, 0, s>>>(m, k);

@@ -158,3 +158,39 @@ def test_tridiagonal_beyond_shared_memory(cuda):
     cols = rng.choice(m, 200, replace=False)
     G = V[:, cols].T @ V[:, cols]
     assert np.max(np.abs(G - np.eye(len(cols)))) <= 1e-8
+
+
+_FORMS = """
+import sys
+sys.path.insert(0, {root!r})
+sys.path.insert(0, {tests!r})
+import numpy as np, torch
+from cmpy_gb300 import engine as E
+import test_gpu_dense_eigh as T
+for n in (200, 300):
+    A = T._rand_sym(n, n + 1)
+    w, V = E.dense_eigh(torch.as_tensor(A).cuda())
+    T._check(A, w, V)
+mats = [T._rand_sym(n, 7 * n) for n in (150, 300, 260)]
+for A, (w, V) in zip(mats, E.dense_eigh_batch([torch.as_tensor(a).cuda() for a in mats])):
+    T._check(A, w, V)
+print("forms ok")
+"""
+
+
+@pytest.mark.parametrize("form", ["16", "8", "0"])
+def test_householder_forms(cuda, form):
+    """Orders 150-300 through each Householder form, forced in a fresh process: a cluster of 16
+    CTAs per matrix, of 8 (the portable size, used where 16 cannot be scheduled), and the
+    per-step launches."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    code = _FORMS.format(root=str(root), tests=str(root / "tests"))
+    env = dict(os.environ, CMPY_ED_HH_CLUSTER=form)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "forms ok" in r.stdout
