@@ -2055,12 +2055,17 @@ static ed_status bfp_start(const ed_plan_s* p, BfpRun& r, const double* v0, doub
 // the update kernel of step k; the caller checks and counts the launch
 static ed_status launch_update(const ed_plan_s* p, BfpRun& r, int k, double* alpha, double* beta, cudaStream_t s) {
   const bool vec = (p->dim % 2 == 0) && (((uintptr_t)r.v.R | (uintptr_t)r.W) & 15) == 0;
-  // one wave: four 256-thread blocks per SM (64 registers), two element pairs per thread in flight
-  const int g = std::min(r.L.nparts, p->ctx->num_sms * 4);
+  // one wave: four 256-thread blocks per SM (64 registers), two element pairs per thread in
+  // flight; small vectors take only the blocks that have elements (every block joins the
+  // reduction of the norm, so idle blocks cost time)
+  const int64_t per_block = (int64_t)BT * (vec ? 4 : 1);
+  const int need = (int)std::max<int64_t>(1, std::min<int64_t>((p->dim + per_block - 1) / per_block, 1 << 30));
+  const int g = std::min({r.L.nparts, p->ctx->num_sms * 4, need});
   if (vec)
     k_bfp_update<true><<<g, BT, 0, s>>>(r.v, k, r.W, r.part, r.partmax, beta, alpha, r.st, 0);
   else
-    k_bfp_update<false><<<r.L.nparts, BT, 0, s>>>(r.v, k, r.W, r.part, r.partmax, beta, alpha, r.st, 0);
+    k_bfp_update<false><<<std::min(r.L.nparts, need), BT, 0, s>>>(r.v, k, r.W, r.part, r.partmax, beta, alpha,
+                                                                  r.st, 0);
   return ED_OK;
 }
 
